@@ -1,0 +1,464 @@
+#!/usr/bin/env python
+"""Benchmark: PBF particle-substeps/s of the GB300 substep on the 4M-particle
+large-scale workload (2 m cube, h 0.02, 200x200x100 particles, 4 Jacobi
+iterations, 4 substeps per frame, a falling 0.3 m sphere collider re-voxelised
+every frame on a 100^3 grid).
+
+One step = one frame = 4 substeps over all particles (plus the frame's
+collider re-voxelisation). Prints ONE JSON line on rank 0:
+
+  value        particle-substeps/s with all state resident in HBM (CUDA events
+               on the library's stream around K frames, each one CUDA-graph
+               launch of 4 substeps + one device voxelisation);
+  e2e          the same metric through the C ABI with host buffers: every
+               frame uploads the host-voxelised collider grid from pinned
+               memory and downloads all particle positions to pinned memory;
+  roofline     the dominant kernel's algorithmic bytes per launch / its mean
+               launch time (CUDA events, launch by launch, same state, same
+               stream) against the measured HBM copy bandwidth;
+  cpu_baseline the oracle's C restatement of the reference passes (OpenMP,
+               all host cores) on a bounded sample of the same workload.
+
+``--impl reference`` times the reference's algorithm on the host cores instead
+(the oracle port: the reference's own GLSL passes need a graphics stack that
+neither machine has), printing the same metric with "impl": "reference".
+
+Multi-GPU: the path does not shard (one domain per scene); under torchrun each
+rank runs an independent replica, the time is the max over ranks and value is
+the sum of all replicas' particle-substeps ("replicas only", weak scaling).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "PBF particle-substeps/s (4M particles, 4 Jacobi iterations)"
+UNIT = "particle-substeps/s"
+
+# Algorithmic bytes per particle and launch of each kernel (compulsory HBM
+# traffic: every array touched once per launch, neighbour reuse served on chip;
+# float4 pos/vel/pred/normal, float2 (density, lambda) of which the kernel
+# needs the lanes it reads, u32 keys/ids/ranks, u64 sort pairs).
+BYTES_PER_PARTICLE = {
+    "normal": 16 + 4 + 16,            # pred, density_j, normal out
+    "predict_key": 16 + 16 + 16 + 4 + 4,  # pos, vel, normal; key, rank out
+    "scatter": 4 + 4 + 4 + 8,         # key, rank, id; pair out
+    "permute_step": 8 + 16 + 16 + 16 + 4 + 16 + 16 + 4 + 4,  # pair, pos, vel, normal, key; pos, pred, id, key out
+    "lambda": 16 + 8,                 # pred; (density, lambda) out
+    "delta_apply": 16 + 4 + 16,       # pred, lambda_j; pred out
+    "xsph_finalize": 16 + 16 + 4 + 16 + 16,  # pred, pos, density_j; pos, vel out
+    "cell_sort_small": 16,            # pairs in + out
+}
+
+
+def _peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True,
+            )
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread is not None:
+            self.thread.join(timeout=5)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {
+            "sm_mhz": statistics.median(sm) if sm else None,
+            "sm_max_mhz": max(mx) if mx else None,
+            "reasons": reasons,
+            "samples": len(self.rows),
+        }
+
+
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def _workload(args):
+    from flowx_gb300 import scenes
+
+    if args.workload == "large":
+        return scenes.large(cell_rule=args.cell_rule)
+    if args.workload == "pool":
+        return scenes.pool(cell_rule=args.cell_rule)
+    if args.workload == "dam_break":
+        return scenes.dam_break(cell_rule=args.cell_rule)
+    raise SystemExit(f"unknown workload {args.workload}")
+
+
+def _workload_config(scene, args, extra=None):
+    c = scene.config
+    cfg = {
+        "workload": f"{scene.name}: {scene.n} particles, h {c.smoothing_radius} m, cells {c.cell_dims} of "
+                    f"{c.cell_size:.4g} m ({args.cell_rule} rule), {c.iterations} Jacobi iterations, "
+                    f"{scene.substeps_per_frame} substeps/frame at dt {scene.dt:.6f} s",
+        "particles": scene.n,
+        "cells": c.cell_count,
+        "iterations": c.iterations,
+        "substeps_per_step": scene.substeps_per_frame,
+        "surface_tension": c.surface_tension,
+        "collider": f"{scene.collider_dims} voxels of {scene.collider_voxel} m, "
+                    + ("re-voxelised every frame" if scene.animated else "static"),
+        "l2": "inputs larger than L2 (particle state alone is ~10x 129 MB)",
+    }
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+def _oracle_sample(scene, target_s=10.0, max_substeps=4):
+    """Time the oracle (C restatement, OpenMP, all host cores) on the
+    workload's initial state: whole substeps of the full scene until
+    ``target_s`` seconds have passed (at most ``max_substeps``)."""
+    from flowx_gb300 import config as C
+    from oracle import oracle as O
+
+    c = scene.config
+    ic = C.collider_binding(scene.collider_dims, scene.collider_voxel)
+    o = O.Oracle(C.push_constant_values(c, scene.dt, ic), scene.positions, scene.velocities,
+                 collider=scene.collider_grid(0), iterations=c.iterations)
+    o.build_grid(0.0, order=O.ORDER_STABLE)
+    cores = O.max_threads()
+    done, t0 = 0, time.perf_counter()
+    while done < max_substeps:
+        o.substep(scene.dt, order=O.ORDER_STABLE)
+        done += 1
+        if time.perf_counter() - t0 >= target_s:
+            break
+    elapsed = time.perf_counter() - t0
+    return {
+        "value": scene.n * done / elapsed,
+        "unit": UNIT,
+        "cores": cores,
+        "kind": "port",
+        "sample": f"{done} substep(s) of the full {scene.n}-particle workload from its seeded state "
+                  f"({elapsed:.1f} s, oracle C restatement, OpenMP {cores} threads, stable grid order)",
+    }
+
+
+def run_reference(args):
+    """--impl reference: the reference's algorithm on the host cores."""
+    world, rank, _ = _dist()
+    if rank != 0:
+        return 0
+    from flowx_gb300 import config as C
+    from oracle import oracle as O
+
+    oracle_build_ok = True
+    try:
+        O.build()
+    except Exception as exc:  # pragma: no cover - depends on the host toolchain
+        oracle_build_ok = False
+        print(json.dumps({"impl": "reference", "unavailable": f"oracle build failed: {exc}"}))
+        return 0
+    scene = _workload(args)
+    c = scene.config
+    ic = C.collider_binding(scene.collider_dims, scene.collider_voxel)
+    o = O.Oracle(C.push_constant_values(c, scene.dt, ic), scene.positions, scene.velocities,
+                 collider=scene.collider_grid(0), iterations=c.iterations)
+    o.build_grid(0.0, order=O.ORDER_STABLE)
+    cores = O.max_threads()
+    for _ in range(args.warmup):
+        o.substep(scene.dt, order=O.ORDER_STABLE)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.substep(scene.dt, order=O.ORDER_STABLE)
+    elapsed = time.perf_counter() - t0
+    value = scene.n * args.steps / elapsed
+    sample = (f"each step is one substep of the full {scene.n}-particle workload (oracle C restatement of the "
+              f"reference passes, OpenMP {cores} threads); the reference's own GLSL passes need a graphics "
+              f"stack, unavailable on this box")
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": elapsed / args.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": _workload_config(scene, args, {"step": "one substep (host CPU)"}),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "oracle_build": oracle_build_ok,
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_flowx(args):
+    import torch
+
+    world, rank, local = _dist()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from flowx_gb300 import scenes
+    from flowx_gb300.sph import Solver, launch_count
+
+    scene = _workload(args)
+    c = scene.config
+    prims_by_frame = [scene.primitives_at(f) for f in range(args.warmup + args.steps + 1)]
+    samples = scene.surface.sample_count
+    sol = Solver(c, scene.positions, scene.velocities, max_cells=c.cell_count,
+                 max_collider_voxels=int(np.prod(scene.collider_dims)) if scene.collider_dims else 0,
+                 max_surface_samples=samples, device=local)
+    dims = scene.collider_dims
+    dt, nsub = scene.dt, scene.substeps_per_frame
+
+    def voxelize(frame):
+        if dims is not None:
+            sol.voxelize(prims_by_frame[frame], dims, scene.collider_voxel)
+
+    voxelize(0)
+    sol._build_grid(0.0)
+    stream = torch.cuda.ExternalStream(sol.stream(), device=local)
+    frame = 0
+    for _ in range(args.warmup):
+        voxelize(frame)
+        sol.step_substeps(dt, nsub)
+        frame += 1
+    sol.synchronize()
+
+    # ---- timed region: device-resident frames ----
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    sol.synchronize()
+    launches0 = launch_count()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        voxelize(frame)
+        sol.step_substeps(dt, nsub)
+        frame += 1
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = launch_count() - launches0
+    clocks.stop()
+    if world > 1:
+        t = torch.tensor([ms], device=f"cuda:{local}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = scene.n * nsub * args.steps * world / (ms / 1e3)
+
+    # ---- per-kernel times (launch by launch, same state and stream) ----
+    prof = sol.profile(dt, nsub * min(args.steps, 4))
+    total_prof = sum(v[0] for v in prof.values())
+    kernels = {
+        name: {
+            "launches": n,
+            "ms_per_launch": t / n,
+            "share": t / total_prof if total_prof else None,
+            "gbs": (BYTES_PER_PARTICLE[name] * scene.n / (t / n * 1e-3) / 1e9) if name in BYTES_PER_PARTICLE else None,
+        }
+        for name, (t, n) in prof.items()
+    }
+    dominant = max(prof, key=lambda k: prof[k][0])
+    peak, peak_kind = _peaks()
+    dom_bytes = BYTES_PER_PARTICLE.get(dominant, 0) * scene.n
+    dom_ms = prof[dominant][0] / prof[dominant][1]
+    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+    traffic = None
+    traffic_path = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(traffic_path):
+        with open(traffic_path) as f:
+            traffic = json.load(f).get(dominant)
+    roofline = {
+        "bound": "hbm",
+        "kernel": dominant,
+        "achieved": achieved,
+        "peak": peak,
+        "peak_kind": peak_kind,
+        "unit": "GB/s",
+        "frac": achieved / peak,
+        "traffic": traffic,
+        "algorithmic_bytes_per_launch": dom_bytes,
+        "ms_per_launch": dom_ms,
+    }
+
+    # ---- e2e: host buffers through the C ABI ----
+    pinned_pos = torch.empty((scene.n, 4), dtype=torch.float32, pin_memory=True).numpy()
+    grids = []
+    if dims is not None:
+        for f in range(args.steps):
+            g = torch.empty(tuple(reversed(dims)), dtype=torch.uint8, pin_memory=True).numpy()
+            g[...] = scene.collider_grid(frame + f)
+            grids.append(g)
+    import ctypes
+
+    from flowx_gb300 import _lib
+
+    sol.synchronize()
+    t0 = time.perf_counter()
+    for f in range(args.steps):
+        if grids:
+            g = grids[f]
+            d3 = (ctypes.c_int32 * 3)(*dims)
+            _lib.check(sol.lib.flowx_set_collider(sol.ctx, g.ctypes.data, d3, float(scene.collider_voxel)), sol.ctx)
+        sol.step_substeps(dt, nsub)
+        _lib.check(sol.lib.flowx_download(sol.ctx, _lib.BUF["positions"], pinned_pos.ctypes.data,
+                                          pinned_pos.nbytes), sol.ctx)
+    sol.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device=f"cuda:{local}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {
+        "value": scene.n * nsub * args.steps * world / e2e_s,
+        "unit": UNIT,
+        "h2d_bytes_per_step": int(np.prod(dims)) if dims is not None else 0,
+        "d2h_bytes_per_step": int(scene.n * 16),
+    }
+
+    # ---- per-frame splat (reported beside the substep metric) ----
+    sol.update_surface(scene.surface, dt, download=False)
+    sol.synchronize()
+    s0 = torch.cuda.Event(enable_timing=True)
+    s1 = torch.cuda.Event(enable_timing=True)
+    s0.record(stream)
+    reps = 3
+    for _ in range(reps):
+        sol.update_surface(scene.surface, dt, download=False)
+    s1.record(stream)
+    s1.synchronize()
+    splat_ms = s0.elapsed_time(s1) / reps
+    finite = bool(np.isfinite(pinned_pos).all())
+    sol.close()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            cpu = _oracle_sample(scene, target_s=args.cpu_seconds)
+        except Exception as exc:  # pragma: no cover
+            cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {exc}"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC,
+            "value": value,
+            "unit": UNIT,
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": ms / args.steps,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32",
+            "data": "synthetic",
+            "config": _workload_config(scene, args, {"step": "one frame = 4 substeps + collider re-voxelisation",
+                                                    "parallelism": f"replicas x{world}"}),
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": int(launches),
+            "clocks": clocks.summary(),
+            "kernels": kernels,
+            "splat_ms_per_frame": splat_ms,
+            "splat_samples": samples,
+            "state_finite": finite,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["flowx", "reference"], default="flowx")
+    ap.add_argument("--workload", default="large", choices=["large", "pool", "dam_break"])
+    ap.add_argument("--cell-rule", default="h", choices=["h", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        print("bench.py: --warmup below 3 is raised to 3", file=sys.stderr)
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_flowx(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

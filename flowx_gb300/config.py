@@ -416,3 +416,28 @@ def stable_pbf_parameters(spacing: float, h: float, mass: float, rest_density: f
     eps = d * ((1.0 + relaxation_factor) / mass - 1.0)
     k = scorr_for_displacement(h, rest_density, scorr_displacement * h)
     return eps, k
+
+
+def config_from_push(values: dict) -> SolverConfig:
+    """A SolverConfig whose push_constant_values() reproduces ``values``
+    (float32 fields round-trip exactly)."""
+    f_lo, f_hi, f_sph, f_sim = (tuple(float(v) for v in values[k]) for k in ("f_lo", "f_hi", "f_sph", "f_sim"))
+    i_grid, i_sort = values["i_grid"], values["i_sort"]
+    cfg = SolverConfig(
+        lo=f_lo[:3],
+        hi=f_hi[:3],
+        smoothing_radius=f_sph[0],
+        spacing=2.0 * f_hi[3],
+        mass=f_sph[1],
+        rest_density=f_sph[2],
+        cell_size=f_lo[3],
+        cell_dims=tuple(int(v) for v in i_grid[:3]),
+        particle_count=int(values["i_layout"][0]),
+        relaxation=f_sph[3],
+        scorr_strength=bits_float(i_sort[2]),
+        surface_tension=bits_float(i_sort[3]),
+        viscosity=f_sim[0],
+        gravity=f_sim[2],
+        damping=f_sim[3],
+    )
+    return cfg

@@ -1,0 +1,248 @@
+// Internal declarations shared by the CUDA translation units of libflowx.
+//
+// Device-side data layout (HBM):
+//   particle arrays live in *grid order*: slot k holds the particle whose
+//   (cell, id) is the k-th smallest under the last grid build, so the 3x3x3
+//   neighbour stencil of any particle is nine contiguous runs of slots (the
+//   three x-adjacent cells of one (y, z) row are adjacent in memory).
+//   ids[k] maps a slot back to the caller's particle id; every upload and
+//   download goes through that permutation, so callers always see the
+//   reference's id-indexed layout (solver/sph.py:127-152).
+//
+//   float4 pos / vel / pred / normal / delta   (xyz + the reference's w lane)
+//   float2 lam                                 (density, lambda)
+//   uint32 keys[k]                             (global cell index of slot k)
+//   uint32 cell_offset[C + 1]                  (exclusive scan of cell counts:
+//                                               cell c owns [off[c], off[c+1]))
+//   uint8  collider voxels                     (x fastest, 1 = occupied)
+//
+// Several independent scenes ("segments") can share one context: their
+// particles and cells are concatenated and every kernel looks up its
+// segment's parameters in a device table, so one launch per pass serves all
+// scenes. A single scene is a table of one segment.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace flowx {
+
+constexpr int kMaxCellScan = 512;       // shaders/sph_common.glsl:30
+constexpr int kMaxColliderSearch = 2;   // shaders/sph_finalize.glsl:13
+constexpr int kSurfaceCellRadius = 2;   // shaders/surface_splat.glsl:30
+constexpr int kSmallCellSort = 32;      // cells above this go to the block sorter
+
+// Per-segment parameters, resolved on the host from the push-constant block
+// (shaders/sph_common.glsl:10-17). Kernel constants that depend only on the
+// push values (kernel coefficients, speed limit) are computed once on the
+// host in float32, in the same operation order as the reference's shader
+// code, so the device never re-derives them.
+struct SegParams {
+  int p_begin, p_count;        // slots [p_begin, p_begin + p_count)
+  int c_begin, c_count;        // cells [c_begin, c_begin + c_count)
+  int nx, ny, nz;              // i_grid.xyz
+  float lox, loy, loz, cell;   // f_lo
+  float hix, hiy, hiz, radius; // f_hi (solver passes) / surface lo (splat)
+  float h, h2, mass, rest;     // f_sph.x, h*h, f_sph.y, f_sph.z
+  float eps;                   // f_sph.w (relaxation)
+  float visc, dt, gravity, damping;  // f_sim
+  float dtc;                   // max(dt, 1e-6)
+  float scorr_k, sigma;        // i_sort.z / .w as floats
+  float poly6, poly6m6, spiky, visclap, w_q, v_max;
+  int col_nx, col_ny, col_nz;  // i_collider.xyz
+  float voxel;                 // i_collider.w as float; 0 = no collider
+  long long col_begin;         // byte offset of this segment's voxels
+  // splat (surface grid) parameters, only read by the splat kernel
+  int snx, sny, snz;
+  float sspacing;
+  long long s_begin;           // first sample of this segment in the output
+};
+
+// Device pointers of one context's state (all in grid order).
+struct DeviceState {
+  float4 *pos, *pos_alt;    // positions; pos_alt receives the permuted copy
+  float4 *vel, *vel_alt;
+  float4 *pred_a, *pred_b;  // predicted positions (Jacobi ping-pong)
+  float4 *normal, *normal_alt;
+  float4 *delta, *delta_alt;
+  float2 *lam, *lam_alt;
+  float4 *stage;            // staging for uploads / downloads
+  uint32_t *keys, *ids;     // per slot
+  uint32_t *key_tmp, *rank_tmp;  // per old slot during a grid build
+  unsigned long long *pairs, *pairs_tmp;  // (id << 32 | old slot) per new slot
+  uint32_t *counts;         // per cell, zero between builds
+  uint32_t *offsets;        // per cell + 1
+  uint32_t *block_sums;     // scan scratch
+  uint32_t *big_cells;      // [0] = count, then cell indices
+  uint8_t *collider;
+  float *surface;
+  const SegParams *segs;
+  int nseg;
+  int n;                    // total particles
+  int cells;                // total cells
+  int sm_count;             // multiprocessors of the context's device
+};
+
+// Segment of slot k (segments are sorted by p_begin).
+__device__ __forceinline__ int seg_of_slot(const SegParams *__restrict__ segs, int nseg, int k)
+{
+  int lo = 0, hi = nseg - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&segs[mid].p_begin) <= k) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// sph_common.glsl:50-54 (cell_coord) and :56-59 (cell_index), local to the segment.
+__device__ __forceinline__ int3 cell_coord(const SegParams &s, float px, float py, float pz)
+{
+  int3 g;
+  g.x = clampi((int)floorf((px - s.lox) / s.cell), 0, s.nx - 1);
+  g.y = clampi((int)floorf((py - s.loy) / s.cell), 0, s.ny - 1);
+  g.z = clampi((int)floorf((pz - s.loz) / s.cell), 0, s.nz - 1);
+  return g;
+}
+__device__ __forceinline__ int cell_index(const SegParams &s, int3 g)
+{
+  return (g.z * s.ny + g.y) * s.nx + g.x;
+}
+
+// sph_common.glsl:84-91
+__device__ __forceinline__ float w_poly6(float r2, float h2, float coef)
+{
+  if (r2 >= h2) return 0.0f;
+  float d = h2 - r2;
+  return coef * d * d * d;
+}
+// sph_common.glsl:111-118
+__device__ __forceinline__ float w_spiky_grad(float r, float h, float coef)
+{
+  if (r >= h) return 0.0f;
+  float d = h - r;
+  return coef * d * d;
+}
+// sph_common.glsl:121-127
+__device__ __forceinline__ float w_visc_lap(float r, float h, float coef)
+{
+  if (r >= h) return 0.0f;
+  return coef * (h - r);
+}
+
+// Visit the candidate slots of the (2R+1)^3 cells around `base`, in the
+// reference's order (dz, dy, dx, then slot), at most kMaxCellScan slots per
+// cell (sph_lambda.glsl:39-56). Within one (dz, dy) row the x-adjacent cells
+// are adjacent in grid order, so a row is one contiguous run unless one of its
+// cells holds more than kMaxCellScan particles.
+template <int R, class F>
+__device__ __forceinline__ void for_each_candidate(const SegParams &s, const uint32_t *__restrict__ off,
+                                                   int3 base, F &&f)
+{
+#pragma unroll 1
+  for (int dz = -R; dz <= R; ++dz) {
+    const int z = base.z + dz;
+    if (z < 0 || z >= s.nz) continue;
+#pragma unroll 1
+    for (int dy = -R; dy <= R; ++dy) {
+      const int y = base.y + dy;
+      if (y < 0 || y >= s.ny) continue;
+      const int x0 = max(base.x - R, 0), x1 = min(base.x + R, s.nx - 1);
+      const int row = s.c_begin + (z * s.ny + y) * s.nx;
+      const uint32_t a = __ldg(&off[row + x0]);
+      const uint32_t b = __ldg(&off[row + x1 + 1]);
+      if (b - a <= (uint32_t)kMaxCellScan) {
+#pragma unroll 1
+        for (uint32_t k = a; k < b; ++k) f((int)k);
+      } else {
+#pragma unroll 1
+        for (int x = x0; x <= x1; ++x) {
+          const uint32_t cs = __ldg(&off[row + x]);
+          uint32_t ce = __ldg(&off[row + x + 1]);
+          if (ce - cs > (uint32_t)kMaxCellScan) ce = cs + kMaxCellScan;
+#pragma unroll 1
+          for (uint32_t k = cs; k < ce; ++k) f((int)k);
+        }
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ bool collider_occupied(const SegParams &s, const uint8_t *__restrict__ col, int cx,
+                                                  int cy, int cz)
+{
+  if (cx < 0 || cy < 0 || cz < 0 || cx >= s.col_nx || cy >= s.col_ny || cz >= s.col_nz) return false;
+  return col[s.col_begin + ((long long)cz * s.col_ny + cy) * s.col_nx + cx] != 0;
+}
+__device__ __forceinline__ int3 collider_coord(const SegParams &s, float px, float py, float pz)
+{
+  return make_int3((int)floorf((px - s.lox) / s.voxel), (int)floorf((py - s.loy) / s.voxel),
+                   (int)floorf((pz - s.loz) / s.voxel));
+}
+
+// ---- launch wrappers (defined in the kernel translation units) ------------
+// Block sizes are chosen per kernel by the tuner (runtime.cu); 0 = default.
+enum KernelId {
+  K_NORMAL = 0,
+  K_PREDICT_KEY,
+  K_SCAN_REDUCE,
+  K_SCAN_TOP,
+  K_SCAN_DOWN,
+  K_SCATTER,
+  K_CELL_SORT_SMALL,
+  K_CELL_SORT_LARGE,
+  K_PERMUTE_STEP,
+  K_LAMBDA,
+  K_DELTA_APPLY,
+  K_XSPH_FINALIZE,
+  K_SPLAT,
+  K_PREDICT,
+  K_DELTA,
+  K_APPLY,
+  K_VELOCITY,
+  K_XSPH,
+  K_FINALIZE,
+  K_PERMUTE_ALL,
+  K_GATHER,
+  K_SCATTER_IDS,
+  K_VOXELIZE,
+  K_COUNT
+};
+
+extern int g_block[K_COUNT];
+
+// grid build
+void launch_predict_key(const DeviceState &d, const float4 *normal_in, cudaStream_t st);
+void launch_key_only(const DeviceState &d, const float4 *pred, cudaStream_t st);
+void launch_scan(const DeviceState &d, cudaStream_t st);
+void launch_scatter(const DeviceState &d, cudaStream_t st);
+void launch_cell_sort(const DeviceState &d, cudaStream_t st);
+void launch_permute_step(const DeviceState &d, float4 *pred_out, const float4 *normal_in, cudaStream_t st);
+void launch_permute_all(const DeviceState &d, const float4 *pred_in, float4 *pred_out, cudaStream_t st);
+// neighbour passes
+void launch_normal(const DeviceState &d, const float4 *pred, float4 *out, cudaStream_t st);
+void launch_lambda(const DeviceState &d, const float4 *pred, cudaStream_t st);
+void launch_delta_apply(const DeviceState &d, const float4 *pred_in, float4 *pred_out, cudaStream_t st);
+void launch_xsph_finalize(const DeviceState &d, const float4 *pred, const float4 *pos_in, float4 *pos_out,
+                          bool keep_delta, cudaStream_t st);
+void launch_splat_segment(const DeviceState &d, int seg, const float *surface_lo, float spacing,
+                          float kernel_radius, float mass, float rest, const int *dims, float *out,
+                          cudaStream_t st);
+// single reference passes (per-pass API)
+void launch_predict(const DeviceState &d, float4 *pred, cudaStream_t st);
+void launch_delta(const DeviceState &d, const float4 *pred, cudaStream_t st);
+void launch_apply(const DeviceState &d, float4 *pred, cudaStream_t st);
+void launch_velocity(const DeviceState &d, const float4 *pred, cudaStream_t st);
+void launch_xsph(const DeviceState &d, const float4 *pred, cudaStream_t st);
+void launch_finalize(const DeviceState &d, const float4 *pred, cudaStream_t st);
+// layout conversion between caller id order and grid order
+void launch_gather_by_id(const uint32_t *ids, const float4 *src_by_id, float4 *dst_by_slot, int n, cudaStream_t st);
+void launch_scatter_by_id(const uint32_t *ids, const float4 *src_by_slot, float4 *dst_by_id, int n, cudaStream_t st);
+void launch_reorder(const uint32_t *src_slot, const float4 *src, float4 *dst, int n, cudaStream_t st);
+// analytic collider voxeliser
+struct Primitive;
+void launch_voxelize(uint8_t *grid, int nx, int ny, int nz, float ox, float oy, float oz, float voxel,
+                     const void *prims, int nprims, cudaStream_t st);
+
+}  // namespace flowx

@@ -1,0 +1,376 @@
+// Neighbour-grid build: the counting sort that replaces the reference's
+// bitonic key sort (shaders/sph_grid_key.glsl, sph_sort.glsl,
+// sph_cell_clear.glsl, sph_cell_range.glsl, driven by solver/sph.py:482-498).
+//
+//   1. predict_key  - per slot: the predicted position's cell key and its rank
+//                     among the particles sharing that cell, from a
+//                     warp-aggregated atomic on the cell's counter;
+//   2. scan         - exclusive scan of the cell counters into cell offsets
+//                     (three launches: tile sums, top-level scan, tile scan);
+//                     counters are re-zeroed on the way, cells holding more
+//                     than kSmallCellSort particles are listed;
+//   3. scatter      - (id, old slot) to offset[key] + rank;
+//   4. cell_sort    - order each cell by particle id (thread per cell for small
+//                     cells, block per listed large cell), which makes the
+//                     result the deterministic (cell, id) order;
+//   5. permute      - move particle state into the new slot order.
+//
+// The sorted key column, the [start, end) of every cell and each cell's
+// membership equal the reference's; within a cell the reference's bitonic
+// network leaves an arbitrary order, this leaves ascending ids.
+#include "pbf_math.cuh"
+
+namespace flowx {
+
+int g_block[K_COUNT] = {0};
+
+static inline int blk(KernelId k, int def) { return g_block[k] > 0 ? g_block[k] : def; }
+static inline unsigned grid_for(long long n, int b) { return (unsigned)((n + b - 1) / b); }
+
+// ---- 1. predict + key + rank ---------------------------------------------
+__device__ __forceinline__ void count_key(uint32_t *counts, uint32_t key, bool active, uint32_t &rank)
+{
+  const unsigned mask = __ballot_sync(0xffffffffu, active);
+  if (!active) return;
+  const unsigned peers = __match_any_sync(mask, key);
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(peers) - 1;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(&counts[key], (uint32_t)__popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  rank = base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+}
+
+// Fused substep: pos/vel/normal -> key, rank (the predicted position itself is
+// recomputed by the permute, which is cheaper than storing and re-reading it).
+__global__ void k_predict_key(DeviceState d, const float4 *__restrict__ normal_in)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = k < d.n;
+  uint32_t key = 0;
+  if (active) {
+    const SegParams &s = d.segs[seg_of_slot(d.segs, d.nseg, k)];
+    const float4 p = d.pos[k];
+    const float4 v = d.vel[k];
+    const float4 n = s.sigma > 0.0f ? normal_in[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float3 vo, q;
+    predict_particle(s, p, v, n, vo, q);
+    key = (uint32_t)(s.c_begin + cell_index(s, cell_coord(s, q.x, q.y, q.z)));
+    d.key_tmp[k] = key;
+  }
+  uint32_t rank = 0;
+  count_key(d.counts, key, active, rank);
+  if (active) d.rank_tmp[k] = rank;
+}
+
+// Key from an already-predicted position (flowx_build_grid after a separate
+// predict, or a seed's zero-length build: solver/sph.py:606).
+__global__ void k_key_only(DeviceState d, const float4 *__restrict__ pred)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = k < d.n;
+  uint32_t key = 0;
+  if (active) {
+    const SegParams &s = d.segs[seg_of_slot(d.segs, d.nseg, k)];
+    const float4 q = pred[k];
+    key = (uint32_t)(s.c_begin + cell_index(s, cell_coord(s, q.x, q.y, q.z)));
+    d.key_tmp[k] = key;
+  }
+  uint32_t rank = 0;
+  count_key(d.counts, key, active, rank);
+  if (active) d.rank_tmp[k] = rank;
+}
+
+void launch_predict_key(const DeviceState &d, const float4 *normal_in, cudaStream_t st)
+{
+  const int b = blk(K_PREDICT_KEY, 256);
+  if (d.n > 0) k_predict_key<<<grid_for(d.n, b), b, 0, st>>>(d, normal_in);
+}
+
+void launch_key_only(const DeviceState &d, const float4 *pred, cudaStream_t st)
+{
+  const int b = blk(K_PREDICT_KEY, 256);
+  if (d.n > 0) k_key_only<<<grid_for(d.n, b), b, 0, st>>>(d, pred);
+}
+
+// ---- 2. exclusive scan of the cell counters -----------------------------
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t &total)
+{
+  __shared__ uint32_t warp_sums[kScanThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_sums[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = lane < kScanThreads / 32 ? warp_sums[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < kScanThreads / 32) warp_sums[lane] = w;
+  }
+  __syncthreads();
+  total = warp_sums[kScanThreads / 32 - 1];
+  const uint32_t warp_prefix = warp > 0 ? warp_sums[warp - 1] : 0u;
+  __syncthreads();
+  return warp_prefix + x - v;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const uint32_t *__restrict__ counts, int cells,
+                                                              uint32_t *__restrict__ block_sums)
+{
+  const long long base = (long long)blockIdx.x * kScanTile;
+  uint32_t local = 0;
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    long long c = base + (long long)j * kScanThreads + threadIdx.x;
+    if (c < cells) local += counts[c];
+  }
+  uint32_t total;
+  block_exclusive_scan(local, total);
+  if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+}
+
+// One block: exclusive scan of the tile sums in place; offsets[cells] = total;
+// resets the large-cell list.
+__global__ void __launch_bounds__(kScanThreads) k_scan_top(uint32_t *__restrict__ block_sums, int nblocks,
+                                                           uint32_t *__restrict__ offsets, int cells,
+                                                           uint32_t *__restrict__ big_cells)
+{
+  uint32_t carry = 0;
+  for (int base = 0; base < nblocks; base += kScanThreads) {
+    const int i = base + threadIdx.x;
+    const uint32_t v = i < nblocks ? block_sums[i] : 0u;
+    uint32_t total;
+    const uint32_t ex = block_exclusive_scan(v, total);
+    if (i < nblocks) block_sums[i] = carry + ex;
+    carry += total;
+  }
+  if (threadIdx.x == 0) {
+    offsets[cells] = carry;
+    big_cells[0] = 0;
+  }
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_down(uint32_t *__restrict__ counts, int cells,
+                                                            const uint32_t *__restrict__ block_sums,
+                                                            uint32_t *__restrict__ offsets,
+                                                            uint32_t *__restrict__ big_cells)
+{
+  // Each thread owns kScanItems consecutive cells of the tile.
+  const long long base = (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanItems;
+  uint32_t v[kScanItems];
+  uint32_t local = 0;
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    const long long c = base + j;
+    v[j] = c < cells ? counts[c] : 0u;
+    local += v[j];
+  }
+  uint32_t total;
+  uint32_t run = block_exclusive_scan(local, total) + block_sums[blockIdx.x];
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    const long long c = base + j;
+    if (c < cells) {
+      offsets[c] = run;
+      if (v[j] != 0u) counts[c] = 0u;
+      if (v[j] > (uint32_t)kSmallCellSort) {
+        const uint32_t slot = atomicAdd(&big_cells[0], 1u);
+        big_cells[1 + slot] = (uint32_t)c;
+      }
+    }
+    run += v[j];
+  }
+}
+
+void launch_scan(const DeviceState &d, cudaStream_t st)
+{
+  const int cells = d.cells;
+  const int nblocks = (int)grid_for(cells, kScanTile);
+  k_scan_reduce<<<nblocks, kScanThreads, 0, st>>>(d.counts, cells, d.block_sums);
+  k_scan_top<<<1, kScanThreads, 0, st>>>(d.block_sums, nblocks, d.offsets, cells, d.big_cells);
+  k_scan_down<<<nblocks, kScanThreads, 0, st>>>(d.counts, cells, d.block_sums, d.offsets, d.big_cells);
+}
+
+// ---- 3. scatter ---------------------------------------------------------
+__global__ void k_scatter(DeviceState d)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= d.n) return;
+  const uint32_t key = d.key_tmp[k];
+  const uint32_t slot = d.offsets[key] + d.rank_tmp[k];
+  d.pairs[slot] = ((unsigned long long)d.ids[k] << 32) | (unsigned long long)(uint32_t)k;
+}
+
+void launch_scatter(const DeviceState &d, cudaStream_t st)
+{
+  const int b = blk(K_SCATTER, 256);
+  if (d.n > 0) k_scatter<<<grid_for(d.n, b), b, 0, st>>>(d);
+}
+
+// ---- 4. order each cell by id -------------------------------------------
+// Small cells: one thread sorts its cell's (id, slot) pairs in registers with
+// an odd-even transposition network of the smallest width in {4, 8, 16, 32}
+// that holds the cell (data-independent control flow keeps the array in
+// registers; padding ~0 sorts last).
+template <int W>
+__device__ __forceinline__ void sort_cell_net(unsigned long long *__restrict__ pairs, uint32_t a, uint32_t n)
+{
+  unsigned long long v[W];
+#pragma unroll
+  for (int j = 0; j < W; ++j) v[j] = (uint32_t)j < n ? pairs[a + j] : ~0ull;
+#pragma unroll
+  for (int round = 0; round < W; ++round) {
+#pragma unroll
+    for (int j = round & 1; j + 1 < W; j += 2) {
+      const unsigned long long x = v[j], y = v[j + 1];
+      v[j] = x < y ? x : y;
+      v[j + 1] = x < y ? y : x;
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < W; ++j)
+    if ((uint32_t)j < n) pairs[a + j] = v[j];
+}
+
+__global__ void k_cell_sort_small(DeviceState d)
+{
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= d.cells) return;
+  const uint32_t a = d.offsets[c];
+  const uint32_t n = d.offsets[c + 1] - a;
+  if (n < 2u) return;
+  if (n <= 4u) sort_cell_net<4>(d.pairs, a, n);
+  else if (n <= 8u) sort_cell_net<8>(d.pairs, a, n);
+  else if (n <= 16u) sort_cell_net<16>(d.pairs, a, n);
+  else if (n <= (uint32_t)kSmallCellSort) sort_cell_net<32>(d.pairs, a, n);
+}
+
+// Large cells (listed by the scan): a block ranks each element against all
+// others of its cell (ids are unique, so ranks are a permutation), writes to
+// the scratch copy and copies back. O(n^2 / blockDim) per cell.
+__global__ void __launch_bounds__(256) k_cell_sort_large(DeviceState d)
+{
+  const uint32_t count = d.big_cells[0];
+  for (uint32_t item = blockIdx.x; item < count; item += gridDim.x) {
+    const uint32_t c = d.big_cells[1 + item];
+    const uint32_t a = d.offsets[c], n = d.offsets[c + 1] - a;
+    for (uint32_t e = threadIdx.x; e < n; e += blockDim.x) {
+      const unsigned long long mine = d.pairs[a + e];
+      uint32_t rank = 0;
+      for (uint32_t f = 0; f < n; ++f) rank += d.pairs[a + f] < mine ? 1u : 0u;
+      d.pairs_tmp[a + rank] = mine;
+    }
+    __syncthreads();
+    for (uint32_t e = threadIdx.x; e < n; e += blockDim.x) d.pairs[a + e] = d.pairs_tmp[a + e];
+    __syncthreads();
+  }
+}
+
+void launch_cell_sort(const DeviceState &d, cudaStream_t st)
+{
+  const int b = blk(K_CELL_SORT_SMALL, 128);
+  if (d.cells > 0) k_cell_sort_small<<<grid_for(d.cells, b), b, 0, st>>>(d);
+  k_cell_sort_large<<<d.sm_count, 256, 0, st>>>(d);
+}
+
+// ---- 5. permute ---------------------------------------------------------
+// Fused substep: new slot k takes old slot s. Positions are copied, the
+// predicted position recomputed from (pos, vel, normal) exactly as predict did,
+// the substep's normal (computed into scratch in the old order) moved to the
+// new slot, and the slot's key and id recorded. Velocity and lambda need no
+// copy: the rest of the substep rewrites them before reading.
+__global__ void k_permute_step(DeviceState d, float4 *__restrict__ pred_out, const float4 *__restrict__ normal_in)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= d.n) return;
+  const unsigned long long pr = d.pairs[k];
+  const int s = (int)(uint32_t)pr;
+  const SegParams &sp = d.segs[seg_of_slot(d.segs, d.nseg, k)];
+  const float4 p = d.pos[s];
+  const float4 v = d.vel[s];
+  const float4 n = sp.sigma > 0.0f ? normal_in[s] : make_float4(0.f, 0.f, 0.f, 0.f);
+  float3 vo, q;
+  predict_particle(sp, p, v, n, vo, q);
+  if (sp.sigma > 0.0f) d.normal[k] = n;
+  d.pos_alt[k] = p;
+  pred_out[k] = make_float4(q.x, q.y, q.z, 1.0f);
+  d.ids[k] = (uint32_t)(pr >> 32);
+  d.keys[k] = d.key_tmp[s];
+}
+
+void launch_permute_step(const DeviceState &d, float4 *pred_out, const float4 *normal_in, cudaStream_t st)
+{
+  const int b = blk(K_PERMUTE_STEP, 256);
+  if (d.n > 0) k_permute_step<<<grid_for(d.n, b), b, 0, st>>>(d, pred_out, normal_in);
+}
+
+// Standalone grid build: every per-particle array moves to its new slot
+// (into the *_alt arrays; the caller copies them back).
+__global__ void k_permute_all(DeviceState d, const float4 *__restrict__ pred_in, float4 *__restrict__ pred_out)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= d.n) return;
+  const unsigned long long pr = d.pairs[k];
+  const int s = (int)(uint32_t)pr;
+  d.pos_alt[k] = d.pos[s];
+  d.vel_alt[k] = d.vel[s];
+  pred_out[k] = pred_in[s];
+  d.normal_alt[k] = d.normal[s];
+  d.delta_alt[k] = d.delta[s];
+  d.lam_alt[k] = d.lam[s];
+  d.ids[k] = (uint32_t)(pr >> 32);
+  d.keys[k] = d.key_tmp[s];
+}
+
+void launch_permute_all(const DeviceState &d, const float4 *pred_in, float4 *pred_out, cudaStream_t st)
+{
+  const int b = blk(K_PERMUTE_ALL, 256);
+  if (d.n > 0) k_permute_all<<<grid_for(d.n, b), b, 0, st>>>(d, pred_in, pred_out);
+}
+
+// ---- layout conversion --------------------------------------------------
+__global__ void k_gather_by_id(const uint32_t *__restrict__ ids, const float4 *__restrict__ src,
+                               float4 *__restrict__ dst, int n)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) dst[k] = src[ids[k]];
+}
+__global__ void k_scatter_by_id(const uint32_t *__restrict__ ids, const float4 *__restrict__ src,
+                                float4 *__restrict__ dst, int n)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) dst[ids[k]] = src[k];
+}
+__global__ void k_reorder(const uint32_t *__restrict__ src_slot, const float4 *__restrict__ src,
+                          float4 *__restrict__ dst, int n)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) dst[k] = src[src_slot[k]];
+}
+
+void launch_gather_by_id(const uint32_t *ids, const float4 *src, float4 *dst, int n, cudaStream_t st)
+{
+  if (n > 0) k_gather_by_id<<<grid_for(n, 256), 256, 0, st>>>(ids, src, dst, n);
+}
+void launch_scatter_by_id(const uint32_t *ids, const float4 *src, float4 *dst, int n, cudaStream_t st)
+{
+  if (n > 0) k_scatter_by_id<<<grid_for(n, 256), 256, 0, st>>>(ids, src, dst, n);
+}
+void launch_reorder(const uint32_t *src_slot, const float4 *src, float4 *dst, int n, cudaStream_t st)
+{
+  if (n > 0) k_reorder<<<grid_for(n, 256), 256, 0, st>>>(src_slot, src, dst, n);
+}
+
+}  // namespace flowx

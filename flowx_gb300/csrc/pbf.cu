@@ -1,0 +1,324 @@
+// PBF passes on the grid-ordered state: the fused substep kernels and the
+// single reference passes (for the per-pass API), plus the per-frame density
+// splat and the analytic collider voxeliser.
+//
+// Fused substep (solver/sph.py:501-514 as executed here):
+//   normal          sph_normal.glsl                      (if sigma > 0)
+//   predict_key     sph_predict.glsl + sph_grid_key.glsl (grid.cu)
+//   scan/scatter/sort/permute                             (grid.cu)
+//   I x { lambda    sph_lambda.glsl
+//         delta_apply sph_delta.glsl + sph_apply_delta.glsl, written to the
+//                     other predicted buffer (ping-pong) }
+//   xsph_finalize   sph_velocity.glsl + sph_xsph.glsl + sph_finalize.glsl:
+//                   neighbour velocities are re-derived from (pred - pos)/dt,
+//                   the same expression sph_velocity.glsl stores, and the new
+//                   positions go to the other position buffer so neighbours
+//                   still read the old ones.
+#include "pbf_math.cuh"
+
+namespace flowx {
+
+static inline int blk(KernelId k, int def) { return g_block[k] > 0 ? g_block[k] : def; }
+static inline unsigned grid_for(long long n, int b) { return (unsigned)((n + b - 1) / b); }
+
+#define FLOWX_SLOT_PROLOGUE                          \
+  const int i = blockIdx.x * blockDim.x + threadIdx.x; \
+  if (i >= d.n) return;                                \
+  const SegParams &s = d.segs[seg_of_slot(d.segs, d.nseg, i)];
+
+// ---- neighbour passes ---------------------------------------------------
+__global__ void __launch_bounds__(256) k_normal(DeviceState d, const float4 *__restrict__ pred,
+                                                float4 *__restrict__ out)
+{
+  FLOWX_SLOT_PROLOGUE
+  out[i] = normal_particle(s, d.offsets, pred, d.lam, i);
+}
+
+__global__ void __launch_bounds__(256) k_lambda(DeviceState d, const float4 *__restrict__ pred)
+{
+  FLOWX_SLOT_PROLOGUE
+  d.lam[i] = lambda_particle(s, d.offsets, pred, i);
+}
+
+// sph_delta.glsl + sph_apply_delta.glsl: pred_out = pred_in + sum / rho0.
+__global__ void __launch_bounds__(256) k_delta_apply(DeviceState d, const float4 *__restrict__ pred_in,
+                                                     float4 *__restrict__ pred_out)
+{
+  FLOWX_SLOT_PROLOGUE
+  const float3 a = delta_sum(s, d.offsets, pred_in, d.lam, i);
+  const float rest = s.rest;
+  const float4 p = pred_in[i];
+  pred_out[i] = make_float4(p.x + a.x / rest, p.y + a.y / rest, p.z + a.z / rest, 1.0f);
+}
+
+// sph_velocity.glsl:20-23 for one slot.
+__device__ __forceinline__ float3 slot_velocity(const float4 &q, const float4 &p, float dtc)
+{
+  return make_float3((q.x - p.x) / dtc, (q.y - p.y) / dtc, (q.z - p.z) / dtc);
+}
+
+// sph_xsph.glsl:35-81: c * sum (m / rho_j) (v_j - v_i) W(r). Neighbour
+// velocities come from `velj(k)`.
+template <class VelJ>
+__device__ __forceinline__ float3 xsph_sum(const SegParams &s, const uint32_t *__restrict__ off,
+                                           const float4 *__restrict__ pred, const float2 *__restrict__ lam,
+                                           int i, float3 vi, VelJ &&velj)
+{
+  const float4 pi = pred[i];
+  const float h2 = s.h2, mass = s.mass, poly6 = s.poly6;
+  float ax = 0.0f, ay = 0.0f, az = 0.0f;
+  const int3 base = cell_coord(s, pi.x, pi.y, pi.z);
+  for_each_candidate<1>(s, off, base, [&](int k) {
+    if (k == i) return;
+    const float4 pj = __ldg(&pred[k]);
+    const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+    const float r2 = dx * dx + dy * dy + dz * dz;
+    if (r2 >= h2) return;
+    const float rho_j = fmaxf(__ldg(&lam[k].x), 1e-6f);
+    const float3 vj = velj(k, pj);
+    const float w = mass / rho_j;
+    const float wk = w_poly6(r2, h2, poly6);
+    ax += (w * (vj.x - vi.x)) * wk;
+    ay += (w * (vj.y - vi.y)) * wk;
+    az += (w * (vj.z - vi.z)) * wk;
+  });
+  const float c = s.visc;
+  return make_float3(c * ax, c * ay, c * az);
+}
+
+__global__ void __launch_bounds__(256) k_xsph_finalize(DeviceState d, const float4 *__restrict__ pred,
+                                                       const float4 *__restrict__ pos_in,
+                                                       float4 *__restrict__ pos_out, int keep_delta)
+{
+  FLOWX_SLOT_PROLOGUE
+  const float dtc = s.dtc;
+  const float4 q = pred[i];
+  const float3 vi = slot_velocity(q, pos_in[i], dtc);
+  const float3 dv = xsph_sum(s, d.offsets, pred, d.lam, i, vi, [&](int k, const float4 &pj) {
+    return slot_velocity(pj, __ldg(&pos_in[k]), dtc);
+  });
+  float3 v = make_float3(vi.x + dv.x, vi.y + dv.y, vi.z + dv.z);
+  float3 p = make_float3(q.x, q.y, q.z);
+  finalize_particle(s, d.collider, p, v);
+  pos_out[i] = make_float4(p.x, p.y, p.z, 1.0f);
+  d.vel[i] = make_float4(v.x, v.y, v.z, 0.0f);
+  if (keep_delta) d.delta[i] = make_float4(dv.x, dv.y, dv.z, 0.0f);
+}
+
+void launch_normal(const DeviceState &d, const float4 *pred, float4 *out, cudaStream_t st)
+{
+  const int b = blk(K_NORMAL, 128);
+  if (d.n > 0) k_normal<<<grid_for(d.n, b), b, 0, st>>>(d, pred, out);
+}
+void launch_lambda(const DeviceState &d, const float4 *pred, cudaStream_t st)
+{
+  const int b = blk(K_LAMBDA, 128);
+  if (d.n > 0) k_lambda<<<grid_for(d.n, b), b, 0, st>>>(d, pred);
+}
+void launch_delta_apply(const DeviceState &d, const float4 *pred_in, float4 *pred_out, cudaStream_t st)
+{
+  const int b = blk(K_DELTA_APPLY, 128);
+  if (d.n > 0) k_delta_apply<<<grid_for(d.n, b), b, 0, st>>>(d, pred_in, pred_out);
+}
+void launch_xsph_finalize(const DeviceState &d, const float4 *pred, const float4 *pos_in, float4 *pos_out,
+                          bool keep_delta, cudaStream_t st)
+{
+  const int b = blk(K_XSPH_FINALIZE, 128);
+  if (d.n > 0) k_xsph_finalize<<<grid_for(d.n, b), b, 0, st>>>(d, pred, pos_in, pos_out, keep_delta ? 1 : 0);
+}
+
+// ---- single reference passes (per-pass API) ------------------------------
+// sph_predict.glsl:23-57
+__global__ void k_predict(DeviceState d, float4 *__restrict__ pred)
+{
+  FLOWX_SLOT_PROLOGUE
+  const float4 n = s.sigma > 0.0f ? d.normal[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+  float3 vo, q;
+  predict_particle(s, d.pos[i], d.vel[i], n, vo, q);
+  d.vel[i] = make_float4(vo.x, vo.y, vo.z, 0.0f);
+  pred[i] = make_float4(q.x, q.y, q.z, 1.0f);
+}
+// sph_delta.glsl:19-85
+__global__ void __launch_bounds__(256) k_delta(DeviceState d, const float4 *__restrict__ pred)
+{
+  FLOWX_SLOT_PROLOGUE
+  const float3 a = delta_sum(s, d.offsets, pred, d.lam, i);
+  const float rest = s.rest;
+  d.delta[i] = make_float4(a.x / rest, a.y / rest, a.z / rest, 0.0f);
+}
+// sph_apply_delta.glsl:10-20
+__global__ void k_apply(DeviceState d, float4 *__restrict__ pred)
+{
+  FLOWX_SLOT_PROLOGUE
+  (void)s;
+  const float4 p = pred[i], dl = d.delta[i];
+  pred[i] = make_float4(p.x + dl.x, p.y + dl.y, p.z + dl.z, 1.0f);
+}
+// sph_velocity.glsl:12-24
+__global__ void k_velocity(DeviceState d, const float4 *__restrict__ pred)
+{
+  FLOWX_SLOT_PROLOGUE
+  const float3 v = slot_velocity(pred[i], d.pos[i], s.dtc);
+  d.vel[i] = make_float4(v.x, v.y, v.z, 0.0f);
+}
+// sph_xsph.glsl:28-82
+__global__ void __launch_bounds__(256) k_xsph(DeviceState d, const float4 *__restrict__ pred)
+{
+  FLOWX_SLOT_PROLOGUE
+  const float4 vi4 = d.vel[i];
+  const float3 vi = make_float3(vi4.x, vi4.y, vi4.z);
+  const float4 *__restrict__ vel = d.vel;
+  const float3 dv = xsph_sum(s, d.offsets, pred, d.lam, i, vi, [&](int k, const float4 &) {
+    const float4 v = __ldg(&vel[k]);
+    return make_float3(v.x, v.y, v.z);
+  });
+  d.delta[i] = make_float4(dv.x, dv.y, dv.z, 0.0f);
+}
+// sph_finalize.glsl:15-96
+__global__ void k_finalize(DeviceState d, const float4 *__restrict__ pred)
+{
+  FLOWX_SLOT_PROLOGUE
+  const float4 v4 = d.vel[i], dl = d.delta[i], q = pred[i];
+  float3 v = make_float3(v4.x + dl.x, v4.y + dl.y, v4.z + dl.z);
+  float3 p = make_float3(q.x, q.y, q.z);
+  finalize_particle(s, d.collider, p, v);
+  d.pos[i] = make_float4(p.x, p.y, p.z, 1.0f);
+  d.vel[i] = make_float4(v.x, v.y, v.z, 0.0f);
+}
+
+void launch_predict(const DeviceState &d, float4 *pred, cudaStream_t st)
+{
+  if (d.n > 0) k_predict<<<grid_for(d.n, 256), 256, 0, st>>>(d, pred);
+}
+void launch_delta(const DeviceState &d, const float4 *pred, cudaStream_t st)
+{
+  const int b = blk(K_DELTA, 128);
+  if (d.n > 0) k_delta<<<grid_for(d.n, b), b, 0, st>>>(d, pred);
+}
+void launch_apply(const DeviceState &d, float4 *pred, cudaStream_t st)
+{
+  if (d.n > 0) k_apply<<<grid_for(d.n, 256), 256, 0, st>>>(d, pred);
+}
+void launch_velocity(const DeviceState &d, const float4 *pred, cudaStream_t st)
+{
+  if (d.n > 0) k_velocity<<<grid_for(d.n, 256), 256, 0, st>>>(d, pred);
+}
+void launch_xsph(const DeviceState &d, const float4 *pred, cudaStream_t st)
+{
+  const int b = blk(K_XSPH, 128);
+  if (d.n > 0) k_xsph<<<grid_for(d.n, b), b, 0, st>>>(d, pred);
+}
+void launch_finalize(const DeviceState &d, const float4 *pred, cudaStream_t st)
+{
+  if (d.n > 0) k_finalize<<<grid_for(d.n, 256), 256, 0, st>>>(d, pred);
+}
+
+// ---- per-frame density splat (surface_splat.glsl:32-97) -----------------
+// One thread per lattice sample of one segment's surface grid; gathers the
+// particles of the 5x5x5 cells around the sample's (clamped) cell.
+struct SplatParams {
+  float slox, sloy, sloz, spacing;
+  float kh2, kcoef, mass, rest;
+  int snx, sny, snz;
+  int seg;
+};
+
+__global__ void __launch_bounds__(256) k_splat(DeviceState d, SplatParams sp, long long samples,
+                                               float *__restrict__ out)
+{
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= samples) return;
+  const SegParams &s = d.segs[sp.seg];
+  const int gx = (int)(t % sp.snx);
+  const int gy = (int)((t / sp.snx) % sp.sny);
+  const int gz = (int)(t / ((long long)sp.snx * sp.sny));
+  const float px = sp.slox + (float)gx * sp.spacing;
+  const float py = sp.sloy + (float)gy * sp.spacing;
+  const float pz = sp.sloz + (float)gz * sp.spacing;
+  const float h2 = sp.kh2, coef = sp.kcoef, mass = sp.mass;
+  const float4 *__restrict__ pos = d.pos;
+  float density = 0.0f;
+  const int3 base = cell_coord(s, px, py, pz);
+  for_each_candidate<kSurfaceCellRadius>(s, d.offsets, base, [&](int k) {
+    const float4 pj = __ldg(&pos[k]);
+    const float dx = px - pj.x, dy = py - pj.y, dz = pz - pj.z;
+    density += mass * w_poly6(dx * dx + dy * dy + dz * dz, h2, coef);
+  });
+  float value = density / fmaxf(sp.rest, 1e-6f);
+  if (s.voxel > 0.0f) {
+    const int3 c = collider_coord(s, px, py, pz);
+    if (collider_occupied(s, d.collider, c.x, c.y, c.z)) value = 0.0f;
+  }
+  out[t] = value;
+}
+
+void launch_splat_segment(const DeviceState &d, int seg, const float *surface_lo, float spacing,
+                          float kernel_radius, float mass, float rest, const int *dims, float *out,
+                          cudaStream_t st)
+{
+  SplatParams sp;
+  sp.slox = surface_lo[0];
+  sp.sloy = surface_lo[1];
+  sp.sloz = surface_lo[2];
+  sp.spacing = spacing;
+  sp.kh2 = kernel_radius * kernel_radius;
+  // sph_common.glsl:68-71 with the surface kernel radius (surface_splat.glsl:49-53)
+  sp.kcoef = 315.0f / (64.0f * 3.14159265358979323846f * powf(kernel_radius, 9.0f));
+  sp.mass = mass;
+  sp.rest = rest;
+  sp.snx = dims[0];
+  sp.sny = dims[1];
+  sp.snz = dims[2];
+  sp.seg = seg;
+  const long long samples = (long long)dims[0] * dims[1] * dims[2];
+  const int b = blk(K_SPLAT, 128);
+  if (samples > 0) k_splat<<<grid_for(samples, b), b, 0, st>>>(d, sp, samples, out);
+}
+
+// ---- analytic collider voxeliser -----------------------------------------
+// Centre-inside occupancy of spheres, boxes and vertical cylinders, in double
+// precision, on the reference's collider-grid layout (origin at the domain's
+// low corner, x fastest: collision/__init__.py:245-254, :276-290).
+struct DevPrimitive {
+  int kind;  // 0 sphere, 1 box, 2 vertical cylinder (same layout as flowx_primitive)
+  int pad;
+  double a[3], b[3], r;
+};
+
+__global__ void k_voxelize(uint8_t *__restrict__ grid, int nx, int ny, int nz, double ox, double oy, double oz,
+                           double voxel, const DevPrimitive *__restrict__ prims, int nprims)
+{
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long total = (long long)nx * ny * nz;
+  if (t >= total) return;
+  const int x = (int)(t % nx), y = (int)((t / nx) % ny), z = (int)(t / ((long long)nx * ny));
+  const double cx = ox + ((double)x + 0.5) * voxel;
+  const double cy = oy + ((double)y + 0.5) * voxel;
+  const double cz = oz + ((double)z + 0.5) * voxel;
+  uint8_t occ = 0;
+  for (int j = 0; j < nprims; ++j) {
+    const DevPrimitive p = prims[j];
+    if (p.kind == 0) {
+      const double dx = cx - p.a[0], dy = cy - p.a[1], dz = cz - p.a[2];
+      occ |= (dx * dx + dy * dy + dz * dz <= (double)p.r * p.r) ? 1 : 0;
+    } else if (p.kind == 1) {
+      occ |= (cx >= p.a[0] && cx <= p.b[0] && cy >= p.a[1] && cy <= p.b[1] && cz >= p.a[2] && cz <= p.b[2]) ? 1
+                                                                                                           : 0;
+    } else if (p.kind == 2) {
+      const double dx = cx - p.a[0], dy = cy - p.a[1];
+      occ |= (dx * dx + dy * dy <= (double)p.r * p.r && cz >= p.a[2] && cz <= p.b[2]) ? 1 : 0;
+    }
+  }
+  grid[t] = occ;
+}
+
+void launch_voxelize(uint8_t *grid, int nx, int ny, int nz, float ox, float oy, float oz, float voxel,
+                     const void *prims, int nprims, cudaStream_t st)
+{
+  const long long total = (long long)nx * ny * nz;
+  if (total > 0)
+    k_voxelize<<<grid_for(total, 256), 256, 0, st>>>(grid, nx, ny, nz, ox, oy, oz, voxel,
+                                                     (const DevPrimitive *)prims, nprims);
+}
+
+}  // namespace flowx

@@ -1,0 +1,224 @@
+/* flowx.h - C ABI of the GB300 PBF substep library (libflowx.so).
+ *
+ * Drop-in for the GPU compute path of Flow-X's solver: the Blender `gpu`
+ * compute plumbing of solver/gpu_util.py plus the pass sequencing of
+ * solver/sph.py. Every entry point takes plain pointers and sizes, returns an
+ * int status (FLOWX_OK = 0) and never traps; the text of the last failure is
+ * available from flowx_last_error().
+ *
+ * Ownership and ordering: device memory belongs to the context; host buffers
+ * belong to the caller. A context is used from one thread at a time. All work
+ * is ordered on the context's CUDA stream; flowx_download() and
+ * flowx_splat() with a host destination return after the data has arrived.
+ *
+ * Buffer layouts at this boundary are the reference's (solver/sph.py:127-152,
+ * solver/gpu_util.py:28-59), indexed by particle id, as flat arrays without
+ * the reference's 256-wide texture padding:
+ *   POSITIONS, VELOCITIES, PREDICTED, DELTA, NORMAL   N x float4
+ *   LAMBDA                                             N x float4 (density, lambda, 0, 0)
+ *   KEYS                                               S x float4 (cell key, particle id, 0, 0),
+ *                                                      S = next power of two >= N; slots >= N
+ *                                                      are padding (key = cell count)
+ *   CELL_START, CELL_END                               C x float, -1 for an empty cell
+ *   SURFACE                                            samples x float (flowx_splat)
+ * A download may also ask for fewer bytes than the whole buffer: it then
+ * returns the first ones.
+ */
+#ifndef FLOWX_H
+#define FLOWX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FLOWX_ABI_VERSION 1
+
+/* Status codes. */
+enum {
+  FLOWX_OK = 0,
+  FLOWX_ERR_ARG = 1,      /* bad argument, size or layout */
+  FLOWX_ERR_CUDA = 2,     /* a CUDA call failed (text in flowx_last_error) */
+  FLOWX_ERR_STATE = 3,    /* call not valid in the context's current state */
+  FLOWX_ERR_CAPACITY = 4, /* larger than the context was created for */
+};
+
+/* The 128-byte push-constant block, field for field
+ * (shaders/sph_common.glsl:10-17, packed by solver/sph.py:433-461):
+ *   i_layout   = (particle_count, tex_width, tex_width, sorted_count)
+ *   i_grid     = (cells_x, cells_y, cells_z, cell_count)
+ *   i_sort     = (bitonic_k, bitonic_j, floatBitsToInt(scorr_k), floatBitsToInt(surface_tension))
+ *                for the splat: (samples_x, samples_y, samples_z, floatBitsToInt(spacing))
+ *                (shaders/surface_splat.glsl:14)
+ *   f_lo       = (domain_min.xyz, cell_size)
+ *   f_hi       = (domain_max.xyz, particle_radius); for the splat: (surface_lo.xyz, 0)
+ *   f_sph      = (smoothing_radius, particle_mass, rest_density, relaxation_epsilon);
+ *                for the splat f_sph.x is the surface kernel radius
+ *   f_sim      = (viscosity, dt, gravity, boundary_damping)
+ *   i_collider = (collider_dims.xyz, floatBitsToInt(collider_voxel_size)); voxel 0 = none
+ * The bitonic (k, j) lanes and the texture widths are accepted and ignored. */
+typedef struct flowx_push {
+  int32_t i_layout[4];
+  int32_t i_grid[4];
+  int32_t i_sort[4];
+  float f_lo[4];
+  float f_hi[4];
+  float f_sph[4];
+  float f_sim[4];
+  int32_t i_collider[4];
+} flowx_push;
+
+/* Buffer ids (the images of solver/sph.py:127-152 and the splat grid). */
+enum {
+  FLOWX_BUF_POSITIONS = 0,
+  FLOWX_BUF_VELOCITIES = 1,
+  FLOWX_BUF_LAMBDA = 2,
+  FLOWX_BUF_PREDICTED = 3,
+  FLOWX_BUF_DELTA = 4,
+  FLOWX_BUF_NORMAL = 5,
+  FLOWX_BUF_KEYS = 6,
+  FLOWX_BUF_CELL_START = 7,
+  FLOWX_BUF_CELL_END = 8,
+  FLOWX_BUF_SURFACE = 9,
+};
+
+/* Pass ids, numbered as solver/sph.py:_PASSES (154-167) plus the splat.
+ * GRID_KEY, SORT, CELL_CLEAR and CELL_RANGE are not separate passes here:
+ * flowx_build_grid() does all four. */
+enum {
+  FLOWX_PASS_NORMAL = 0,
+  FLOWX_PASS_PREDICT = 1,
+  FLOWX_PASS_GRID_KEY = 2,
+  FLOWX_PASS_SORT = 3,
+  FLOWX_PASS_CELL_CLEAR = 4,
+  FLOWX_PASS_CELL_RANGE = 5,
+  FLOWX_PASS_LAMBDA = 6,
+  FLOWX_PASS_DELTA = 7,
+  FLOWX_PASS_APPLY_DELTA = 8,
+  FLOWX_PASS_VELOCITY = 9,
+  FLOWX_PASS_XSPH = 10,
+  FLOWX_PASS_FINALIZE = 11,
+};
+
+/* Context flags. */
+enum {
+  /* The fused substep also writes the XSPH velocity correction to DELTA, as
+   * the reference's sph_xsph.glsl leaves it (off by default: nothing in the
+   * substep reads it back). */
+  FLOWX_FLAG_KEEP_DELTA = 1,
+};
+
+/* Sizes a context is created for (solver/sph.py:350-369 _allocate). */
+typedef struct flowx_config {
+  int32_t particle_count;       /* N, fixed for the context's lifetime */
+  int32_t max_cells;            /* capacity for i_grid.w */
+  int64_t max_collider_voxels;  /* capacity of the collider grid */
+  int64_t max_surface_samples;  /* capacity of the splat grid */
+  int32_t device;               /* CUDA device ordinal */
+  int32_t flags;                /* FLOWX_FLAG_* */
+} flowx_config;
+
+/* An analytic collider shape for flowx_voxelize(): kind 0 = sphere (a =
+ * centre, r = radius), 1 = axis-aligned box (a = min, b = max), 2 = vertical
+ * cylinder (a = base centre, r = radius, b[2] = top). */
+typedef struct flowx_primitive {
+  int32_t kind;
+  int32_t pad;
+  double a[3];
+  double b[3];
+  double r;
+} flowx_primitive;
+
+typedef struct flowx_ctx flowx_ctx;
+
+/* Create / destroy a context. Replaces solver/sph.py:350-369 (_allocate) and
+ * the texture creation of solver/gpu_util.py:46-59 (make_texture). After
+ * creation every buffer is zero and the positions of a fresh context must be
+ * uploaded before stepping. */
+int flowx_create(const flowx_config *config, flowx_ctx **out);
+int flowx_destroy(flowx_ctx *ctx);
+
+/* Text of the last failure on this context (or of the last failed
+ * flowx_create when ctx is NULL). Never NULL. */
+const char *flowx_last_error(const flowx_ctx *ctx);
+
+/* Host -> device copy of a whole buffer in the reference layout (see the file
+ * header). Replaces solver/gpu_util.py:46-59 (make_texture with values).
+ * Uploading KEYS re-orders the context's particle state to that key order;
+ * the keys must be sorted by cell with ids forming a permutation of 0..N-1.
+ * CELL_START / CELL_END are checked against the uploaded keys. */
+int flowx_upload(flowx_ctx *ctx, int buffer, const void *host, size_t bytes);
+
+/* Device -> host copy in the reference layout. Replaces
+ * solver/gpu_util.py:62-89 (read_texture, read_scalar_texture). */
+int flowx_download(flowx_ctx *ctx, int buffer, void *host, size_t bytes);
+
+/* Install the collider occupancy grid (uint8, x fastest, origin at the
+ * domain's low corner, nonzero = occupied). Replaces the R32F collider texture
+ * of collision/__init__.py:276-290 read as "> 0.5" (sph_common.glsl:154-160).
+ * occupancy NULL or voxel_size 0 removes it. */
+int flowx_set_collider(flowx_ctx *ctx, const uint8_t *occupancy, const int32_t dims[3], float voxel_size);
+
+/* Build the collider grid on the device from analytic shapes (centre-inside
+ * test in double precision). Same layout as flowx_set_collider. No reference
+ * counterpart: the reference voxelises meshes on the CPU
+ * (collision/__init__.py:304-367). */
+int flowx_voxelize(flowx_ctx *ctx, const flowx_primitive *prims, int count, const int32_t dims[3],
+                   float voxel_size, const float origin[3]);
+
+/* The neighbour grid from the current predicted positions: keys, cell ranges
+ * and the particle order. Replaces solver/sph.py:482-498 (_build_grid: the
+ * grid-key pass, the bitonic (k, j) dispatch loop, cell clear, cell range). */
+int flowx_build_grid(flowx_ctx *ctx, const flowx_push *push);
+
+/* One substep with `iterations` Jacobi iterations. Replaces
+ * solver/sph.py:501-514 (_substep); the normal pass runs when the block's
+ * surface tension is > 0, as there. */
+int flowx_substep(flowx_ctx *ctx, const flowx_push *push, int iterations);
+
+/* `substeps` substeps as one CUDA-graph launch (captured on first use for a
+ * given shape). Replaces the substep loop of solver/sph.py:517-530 (_step). */
+int flowx_step(flowx_ctx *ctx, const flowx_push *push, int iterations, int substeps);
+
+/* One reference pass on the current buffers, as one gpu.compute.dispatch of
+ * solver/gpu_util.py:157-159 (dispatch_1d) of that pass would. */
+int flowx_run_pass(flowx_ctx *ctx, int pass_id, const flowx_push *push);
+
+/* The per-frame density splat with the splat's push block (see flowx_push).
+ * Replaces solver/surface.py:201-240 (update: dispatch + read_scalar_texture).
+ * host_out may be NULL to keep the grid on the device (download SURFACE). */
+int flowx_splat(flowx_ctx *ctx, const flowx_push *splat_push, float *host_out, size_t bytes);
+
+/* Wait for all queued work. */
+int flowx_synchronize(flowx_ctx *ctx);
+
+/* The context's CUDA stream (a cudaStream_t), for callers that order their
+ * own work or events against it. */
+int flowx_get_stream(flowx_ctx *ctx, void **stream);
+
+/* Device time in milliseconds of `steps` flowx_step() calls (graph launches),
+ * measured with CUDA events on the context's stream after one untimed warm-up
+ * launch. No reference counterpart (the reference times whole frames on the
+ * host, solver/sph.py:517-545). */
+int flowx_time_steps(flowx_ctx *ctx, const flowx_push *push, int iterations, int substeps, int steps,
+                     float *ms);
+
+/* Per-kernel device time: runs `substeps` substeps launch by launch with CUDA
+ * events around every kernel and accumulates milliseconds and launch counts
+ * per kernel id into ms[] / launches[] (arrays of flowx_kernel_count()
+ * entries; names from flowx_kernel_name()). No reference counterpart. */
+int flowx_profile_substeps(flowx_ctx *ctx, const flowx_push *push, int iterations, int substeps, float *ms,
+                           int32_t *launches);
+int flowx_kernel_count(void);
+const char *flowx_kernel_name(int kernel_id);
+
+/* Total number of kernel launches this library has issued (all contexts). */
+int64_t flowx_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FLOWX_H */

@@ -352,7 +352,11 @@ static void pass_delta(const oracle_push *pc, oracle_buffers *b)
       if (scorr_k > 0.0f && w_q > 1e-9f) {
         float ratio = w_poly6(r2, h2, poly6) / w_q;
         float rr = fmaxf(ratio, 0.0f);
-        s_corr = -scorr_k * powf(rr, 4.0f);
+        /* pow(max(ratio, 0), 4.0) (sph_delta.glsl:75), evaluated as two
+         * squarings: GLSL leaves pow's accuracy to the implementation and
+         * an integer power is exact to within one rounding this way. */
+        float rr2 = rr * rr;
+        s_corr = -scorr_k * (rr2 * rr2);
       }
       float s = (lambda_i + lambda_j + s_corr) * w_spiky_grad(r, h, spiky);
       ax += s * (dx / r);
