@@ -431,6 +431,7 @@ def run_flowx(args):
             "gpu_launches": int(launches),
             "clocks": clocks.summary(),
             "kernels": kernels,
+            "math": "fast (re-associated float32; FLOWX_FLAG_EXACT gives the reference's expressions)",
             "splat_ms_per_frame": splat_ms,
             "splat_samples": samples,
             "state_finite": finite,

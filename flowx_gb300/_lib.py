@@ -42,6 +42,7 @@ PASS = {
     "finalize": 11,
 }
 FLAG_KEEP_DELTA = 1
+FLAG_EXACT = 2
 
 
 class Push(ctypes.Structure):

@@ -400,7 +400,7 @@ def scorr_for_displacement(h: float, rest_density: float, displacement: float) -
 
 
 def stable_pbf_parameters(spacing: float, h: float, mass: float, rest_density: float,
-                          relaxation_factor: float = 7.0, scorr_displacement: float = 1e-4):
+                          relaxation_factor: float = 31.0, scorr_displacement: float = 1e-4):
     """(relaxation, scorr_k) for the synthetic workloads.
 
     The reference's update lacks the particle mass in sph_delta.glsl:84, so at
@@ -410,7 +410,11 @@ def stable_pbf_parameters(spacing: float, h: float, mass: float, rest_density: f
     mass-consistent step with a relaxation of ``relaxation_factor`` times the
     lattice denominator D, i.e. eps = D * ((1 + f) / m - 1), and an s_corr
     strength whose per-neighbour correction at h/2 is
-    ``scorr_displacement * h``.
+    ``scorr_displacement * h``. With f = 31 the free-surface particles, whose
+    density constraint the reference does not clamp, stay within a cell of the
+    grid they were sorted into; at f = 7 a few escape it in deep columns,
+    lose their own density term (it drops to the 1e-6 floor) and XSPH then
+    drives their neighbours to ~1e6 m/s.
     """
     d = lattice_constraint_denominator(spacing, h, mass, rest_density)
     eps = d * ((1.0 + relaxation_factor) / mass - 1.0)

@@ -421,10 +421,12 @@ int flowx_profile_substeps(flowx_ctx *ctx, const flowx_push *push, int iteration
     recs.push_back(r);
   };
   const DeviceState &d = c->d;
+  const bool exact = (c->flags & FLOWX_FLAG_EXACT) != 0;
   const int end_idx = iterations % 2 == 0 ? 0 : 1;
   for (int s = 0; s < substeps; ++s) {
     float4 *pin = c->pred_cur();
-    if (c->segs_need_normal()) timed(K_NORMAL, 1, [&] { launch_normal(d, pin, d.normal_alt, c->stream); });
+    if (c->segs_need_normal())
+      timed(K_NORMAL, 1, [&] { launch_normal_f(d, pin, d.normal_alt, exact, c->stream); });
     timed(K_PREDICT_KEY, 1, [&] { launch_predict_key(d, d.normal_alt, c->stream); });
     timed(K_SCAN_REDUCE, 3, [&] { launch_scan(d, c->stream); });
     timed(K_SCATTER, 1, [&] { launch_scatter(d, c->stream); });
@@ -432,12 +434,12 @@ int flowx_profile_substeps(flowx_ctx *ctx, const flowx_push *push, int iteration
     timed(K_PERMUTE_STEP, 1, [&] { launch_permute_step(d, d.pred_a, d.normal_alt, c->stream); });
     float4 *q_in = d.pred_a, *q_out = d.pred_b;
     for (int it = 0; it < iterations; ++it) {
-      timed(K_LAMBDA, 1, [&] { launch_lambda(d, q_in, c->stream); });
-      timed(K_DELTA_APPLY, 1, [&] { launch_delta_apply(d, q_in, q_out, c->stream); });
+      timed(K_LAMBDA, 1, [&] { launch_lambda_f(d, q_in, exact, c->stream); });
+      timed(K_DELTA_APPLY, 1, [&] { launch_delta_apply_f(d, q_in, q_out, exact, c->stream); });
       std::swap(q_in, q_out);
     }
     timed(K_XSPH_FINALIZE, 1, [&] {
-      launch_xsph_finalize(d, q_in, d.pos_alt, d.pos, (c->flags & FLOWX_FLAG_KEEP_DELTA) != 0, c->stream);
+      launch_xsph_finalize_f(d, q_in, d.pos_alt, d.pos, (c->flags & FLOWX_FLAG_KEEP_DELTA) != 0, exact, c->stream);
     });
     c->pred_idx = end_idx;
     c->after_fused_substep();

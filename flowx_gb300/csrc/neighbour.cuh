@@ -1,0 +1,169 @@
+// Two-phase neighbour walk and the pass bodies of the fused substep.
+//
+// The reference scans the 27 cells around every particle in every neighbour
+// pass (sph_lambda.glsl:39-70 and its siblings): ~216 candidates per particle
+// at 8 particles per cell, of which ~15-20% lie within h. On a SIMT machine a
+// per-candidate branch into the pair arithmetic costs the whole warp that
+// arithmetic for nearly every candidate (some lane almost always accepts).
+// So each pass walks its candidates twice, inside one thread:
+//   phase 1 - for each of the nine (dz, dy) rows of the stencil (one
+//             contiguous slot run, the three x-adjacent cells being adjacent
+//             in grid order), set bit t of a 64-bit register mask when slot
+//             a + t passes the pass's own distance test, evaluated with the
+//             very expression the pass body uses;
+//   phase 2 - run the pass body over the set bits, rows in order, slots
+//             ascending.
+// Phase 2 visits exactly the candidates the body would accept, in the
+// reference's (row, slot) order, so the result equals a single scan's. A row
+// longer than 64 slots (dense regions, or a cell above the reference's
+// MAX_CELL_SCAN) is walked directly instead.
+#pragma once
+
+#include "pbf_math.cuh"
+
+namespace flowx {
+
+constexpr int kRows = 9;
+
+template <bool EXACT>
+__device__ __forceinline__ float pair_r2(float dx, float dy, float dz)
+{
+  if (EXACT) return dx * dx + dy * dy + dz * dz;
+  return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+
+// Visit the candidates k of the 3x3x3 stencil around `base` whose position
+// pos[k] satisfies pair_r2<EXACT>(p - pos[k]) < lim2, in the reference's
+// order; `f(k)` is called for each. Rows whose run exceeds 64 slots are
+// walked directly with the reference's per-cell MAX_CELL_SCAN cap, calling
+// f for every candidate of the row (the body repeats its own test).
+template <bool EXACT, class F>
+__device__ __forceinline__ void for_each_within(const SegParams &s, const uint32_t *__restrict__ off,
+                                                const float4 *__restrict__ pos, float4 p, float lim2, int3 base,
+                                                F &&f)
+{
+  const int x0 = max(base.x - 1, 0), x1 = min(base.x + 1, s.nx - 1);
+#pragma unroll 1
+  for (int r = 0; r < kRows; ++r) {
+    const int z = base.z + (r / 3) - 1;
+    const int y = base.y + (r % 3) - 1;
+    if (z < 0 || z >= s.nz || y < 0 || y >= s.ny) continue;
+    const int row = s.c_begin + (z * s.ny + y) * s.nx;
+    const uint32_t ra = __ldg(&off[row + x0]);
+    const uint32_t rb = __ldg(&off[row + x1 + 1]);
+    if (rb - ra > 64u) {
+#pragma unroll 1
+      for (int x = x0; x <= x1; ++x) {
+        const uint32_t cs = __ldg(&off[row + x]);
+        uint32_t ce = __ldg(&off[row + x + 1]);
+        if (ce - cs > (uint32_t)kMaxCellScan) ce = cs + kMaxCellScan;
+#pragma unroll 1
+        for (uint32_t k = cs; k < ce; ++k) f((int)k);
+      }
+      continue;
+    }
+    // phase 1: this row's candidates within reach, as bits
+    unsigned long long mm = 0ull;
+#pragma unroll 4
+    for (uint32_t k = ra; k < rb; ++k) {
+      const float4 q = __ldg(&pos[k]);
+      const float r2 = pair_r2<EXACT>(p.x - q.x, p.y - q.y, p.z - q.z);
+      if (r2 < lim2) mm |= 1ull << (k - ra);
+    }
+    // phase 2: the pass body over them, slots ascending
+#pragma unroll 1
+    while (mm) {
+      const int t = __ffsll((long long)mm) - 1;
+      mm &= mm - 1ull;
+      f((int)ra + t);
+    }
+  }
+}
+
+// ---- pass bodies ----------------------------------------------------------
+// EXACT: the reference's expressions, operation for operation (bit-identical
+// to the oracle). FAST: the same quantities re-associated for throughput (FMA,
+// one reciprocal square root per pair, reciprocal-multiplies for divisions by
+// per-particle constants), within float32 rounding of EXACT.
+
+template <bool EXACT>
+struct LambdaAcc {
+  float density = 0.0f, gx = 0.0f, gy = 0.0f, gz = 0.0f, gn2 = 0.0f;
+
+  // Pairs with r2 >= h2 contribute nothing (sph_lambda.glsl:58-62), so the
+  // walk may skip them.
+  __device__ __forceinline__ void pair(const SegParams &s, float dx, float dy, float dz, bool self)
+  {
+    if (EXACT) {
+      const float r2 = dx * dx + dy * dy + dz * dz;
+      if (r2 >= s.h2) return;
+      density += s.mass * w_poly6(r2, s.h2, s.poly6);
+      if (self || r2 <= 1e-12f) return;
+      const float r = sqrtf(r2);
+      const float sg = s.mass * w_spiky_grad(r, s.h, s.spiky);
+      const float ax = sg * (dx / r), ay = sg * (dy / r), az = sg * (dz / r);
+      gx += ax;
+      gy += ay;
+      gz += az;
+      gn2 += ax * ax + ay * ay + az * az;
+    } else {
+      const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+      if (r2 >= s.h2) return;
+      const float t = __fsub_rn(s.h2, r2);
+      density = __fmaf_rn(__fmul_rn(t, t), t, density);  // scaled by mass * poly6 at the end
+      if (self || r2 <= 1e-12f) return;
+      const float rinv = rsqrtf(r2);
+      const float hr = __fsub_rn(s.h, __fmul_rn(r2, rinv));
+      const float g = __fmul_rn(__fmul_rn(s.mass * s.spiky, __fmul_rn(hr, hr)), rinv);
+      gx = __fmaf_rn(g, dx, gx);
+      gy = __fmaf_rn(g, dy, gy);
+      gz = __fmaf_rn(g, dz, gz);
+      gn2 = __fmaf_rn(__fmul_rn(g, g), r2, gn2);
+    }
+  }
+
+  __device__ __forceinline__ float2 finish(const SegParams &s) const
+  {
+    const float rest = s.rest;
+    const float dens = EXACT ? density : __fmul_rn(density, s.mass * s.poly6);
+    const float constraint = fmaxf(dens, 1e-6f) / rest - 1.0f;
+    const float denom = (gx * gx + gy * gy + gz * gz + gn2) / (rest * rest) + s.eps;
+    return make_float2(fmaxf(dens, 1e-6f), -constraint / fmaxf(denom, 1e-9f));
+  }
+};
+
+template <bool EXACT>
+__device__ __forceinline__ void delta_pair(const SegParams &s, float lambda_i, float lambda_j, float dx, float dy,
+                                           float dz, float r2, float &ax, float &ay, float &az)
+{
+  if (EXACT) {
+    const float r = sqrtf(r2);
+    float s_corr = 0.0f;
+    if (s.scorr_k > 0.0f && s.w_q > 1e-9f) {
+      const float ratio = w_poly6(r2, s.h2, s.poly6) / s.w_q;
+      const float rr = fmaxf(ratio, 0.0f);
+      const float rr2 = rr * rr;
+      s_corr = -s.scorr_k * (rr2 * rr2);
+    }
+    const float sc = (lambda_i + lambda_j + s_corr) * w_spiky_grad(r, s.h, s.spiky);
+    ax += sc * (dx / r);
+    ay += sc * (dy / r);
+    az += sc * (dz / r);
+  } else {
+    const float rinv = rsqrtf(r2);
+    const float hr = __fsub_rn(s.h, __fmul_rn(r2, rinv));
+    float lam = __fadd_rn(lambda_i, lambda_j);
+    if (s.scorr_k > 0.0f && s.w_q > 1e-9f) {
+      const float t = __fsub_rn(s.h2, r2);
+      const float ratio = __fmul_rn(__fmul_rn(__fmul_rn(t, t), t), s.poly6 / s.w_q);
+      const float rr2 = __fmul_rn(ratio, ratio);
+      lam = __fmaf_rn(-s.scorr_k, __fmul_rn(rr2, rr2), lam);
+    }
+    const float sc = __fmul_rn(__fmul_rn(lam, __fmul_rn(s.spiky, __fmul_rn(hr, hr))), rinv);
+    ax = __fmaf_rn(sc, dx, ax);
+    ay = __fmaf_rn(sc, dy, ay);
+    az = __fmaf_rn(sc, dz, az);
+  }
+}
+
+}  // namespace flowx

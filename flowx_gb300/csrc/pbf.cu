@@ -14,42 +14,18 @@
 //                   the same expression sph_velocity.glsl stores, and the new
 //                   positions go to the other position buffer so neighbours
 //                   still read the old ones.
-#include "pbf_math.cuh"
+// Every neighbour pass uses the two-phase walk of neighbour.cuh.
+#include "neighbour.cuh"
 
 namespace flowx {
 
 static inline int blk(KernelId k, int def) { return g_block[k] > 0 ? g_block[k] : def; }
 static inline unsigned grid_for(long long n, int b) { return (unsigned)((n + b - 1) / b); }
 
-#define FLOWX_SLOT_PROLOGUE                          \
+#define FLOWX_SLOT_PROLOGUE                            \
   const int i = blockIdx.x * blockDim.x + threadIdx.x; \
   if (i >= d.n) return;                                \
   const SegParams &s = d.segs[seg_of_slot(d.segs, d.nseg, i)];
-
-// ---- neighbour passes ---------------------------------------------------
-__global__ void __launch_bounds__(256) k_normal(DeviceState d, const float4 *__restrict__ pred,
-                                                float4 *__restrict__ out)
-{
-  FLOWX_SLOT_PROLOGUE
-  out[i] = normal_particle(s, d.offsets, pred, d.lam, i);
-}
-
-__global__ void __launch_bounds__(256) k_lambda(DeviceState d, const float4 *__restrict__ pred)
-{
-  FLOWX_SLOT_PROLOGUE
-  d.lam[i] = lambda_particle(s, d.offsets, pred, i);
-}
-
-// sph_delta.glsl + sph_apply_delta.glsl: pred_out = pred_in + sum / rho0.
-__global__ void __launch_bounds__(256) k_delta_apply(DeviceState d, const float4 *__restrict__ pred_in,
-                                                     float4 *__restrict__ pred_out)
-{
-  FLOWX_SLOT_PROLOGUE
-  const float3 a = delta_sum(s, d.offsets, pred_in, d.lam, i);
-  const float rest = s.rest;
-  const float4 p = pred_in[i];
-  pred_out[i] = make_float4(p.x + a.x / rest, p.y + a.y / rest, p.z + a.z / rest, 1.0f);
-}
 
 // sph_velocity.glsl:20-23 for one slot.
 __device__ __forceinline__ float3 slot_velocity(const float4 &q, const float4 &p, float dtc)
@@ -57,45 +33,113 @@ __device__ __forceinline__ float3 slot_velocity(const float4 &q, const float4 &p
   return make_float3((q.x - p.x) / dtc, (q.y - p.y) / dtc, (q.z - p.z) / dtc);
 }
 
-// sph_xsph.glsl:35-81: c * sum (m / rho_j) (v_j - v_i) W(r). Neighbour
-// velocities come from `velj(k)`.
-template <class VelJ>
-__device__ __forceinline__ float3 xsph_sum(const SegParams &s, const uint32_t *__restrict__ off,
-                                           const float4 *__restrict__ pred, const float2 *__restrict__ lam,
-                                           int i, float3 vi, VelJ &&velj)
+// ---- neighbour passes -------------------------------------------------------
+
+// sph_lambda.glsl:17-77
+template <bool EXACT>
+__global__ void __launch_bounds__(256) k_lambda_f(DeviceState d, const float4 *__restrict__ pred)
 {
+  FLOWX_SLOT_PROLOGUE
   const float4 pi = pred[i];
-  const float h2 = s.h2, mass = s.mass, poly6 = s.poly6;
-  float ax = 0.0f, ay = 0.0f, az = 0.0f;
   const int3 base = cell_coord(s, pi.x, pi.y, pi.z);
-  for_each_candidate<1>(s, off, base, [&](int k) {
+  LambdaAcc<EXACT> acc;
+  for_each_within<EXACT>(s, d.offsets, pred, pi, s.h2, base, [&](int k) {
+    const float4 pj = __ldg(&pred[k]);
+    acc.pair(s, pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, k == i);
+  });
+  d.lam[i] = acc.finish(s);
+}
+
+// sph_delta.glsl:19-85, summed correction before the 1/rho0 scale.
+template <bool EXACT>
+__device__ __forceinline__ float3 delta_sum_f(const SegParams &s, const DeviceState &d, const float4 *__restrict__ pred,
+                                              int i, float4 pi)
+{
+  const float lambda_i = d.lam[i].y;
+  const int3 base = cell_coord(s, pi.x, pi.y, pi.z);
+  float ax = 0.0f, ay = 0.0f, az = 0.0f;
+  const float h2 = s.h2;
+  for_each_within<EXACT>(s, d.offsets, pred, pi, h2, base, [&](int k) {
     if (k == i) return;
     const float4 pj = __ldg(&pred[k]);
     const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-    const float r2 = dx * dx + dy * dy + dz * dz;
+    const float r2 = pair_r2<EXACT>(dx, dy, dz);
+    if (r2 >= h2 || r2 <= 1e-12f) return;
+    delta_pair<EXACT>(s, lambda_i, __ldg(&d.lam[k].y), dx, dy, dz, r2, ax, ay, az);
+  });
+  return make_float3(ax, ay, az);
+}
+
+// sph_delta.glsl + sph_apply_delta.glsl: pred_out = pred_in + sum / rho0.
+template <bool EXACT>
+__global__ void __launch_bounds__(256) k_delta_apply_f(DeviceState d, const float4 *__restrict__ pred_in,
+                                                       float4 *__restrict__ pred_out)
+{
+  FLOWX_SLOT_PROLOGUE
+  const float4 pi = pred_in[i];
+  const float3 a = delta_sum_f<EXACT>(s, d, pred_in, i, pi);
+  const float rest = s.rest;
+  pred_out[i] = make_float4(pi.x + a.x / rest, pi.y + a.y / rest, pi.z + a.z / rest, 1.0f);
+}
+
+// sph_xsph.glsl:35-81: c * sum (m / rho_j) (v_j - v_i) W(r), neighbour
+// velocities from velj(k, pred_k).
+template <bool EXACT, class VelJ>
+__device__ __forceinline__ float3 xsph_sum_f(const SegParams &s, const DeviceState &d, const float4 *__restrict__ pred,
+                                             int i, float4 q, float3 vi, VelJ &&velj)
+{
+  const int3 base = cell_coord(s, q.x, q.y, q.z);
+  const float h2 = s.h2, mass = s.mass, poly6 = s.poly6;
+  float ax = 0.0f, ay = 0.0f, az = 0.0f;
+  for_each_within<EXACT>(s, d.offsets, pred, q, h2, base, [&](int k) {
+    if (k == i) return;
+    const float4 pj = __ldg(&pred[k]);
+    const float dx = q.x - pj.x, dy = q.y - pj.y, dz = q.z - pj.z;
+    const float r2 = pair_r2<EXACT>(dx, dy, dz);
     if (r2 >= h2) return;
-    const float rho_j = fmaxf(__ldg(&lam[k].x), 1e-6f);
+    const float rho_j = fmaxf(__ldg(&d.lam[k].x), 1e-6f);
     const float3 vj = velj(k, pj);
-    const float w = mass / rho_j;
-    const float wk = w_poly6(r2, h2, poly6);
-    ax += (w * (vj.x - vi.x)) * wk;
-    ay += (w * (vj.y - vi.y)) * wk;
-    az += (w * (vj.z - vi.z)) * wk;
+    if (EXACT) {
+      const float w = mass / rho_j;
+      const float wk = w_poly6(r2, h2, poly6);
+      ax += (w * (vj.x - vi.x)) * wk;
+      ay += (w * (vj.y - vi.y)) * wk;
+      az += (w * (vj.z - vi.z)) * wk;
+    } else {
+      const float t = __fsub_rn(h2, r2);
+      const float wk = __fmul_rn(__fdividef(mass * poly6, rho_j), __fmul_rn(__fmul_rn(t, t), t));
+      ax = __fmaf_rn(wk, __fsub_rn(vj.x, vi.x), ax);
+      ay = __fmaf_rn(wk, __fsub_rn(vj.y, vi.y), ay);
+      az = __fmaf_rn(wk, __fsub_rn(vj.z, vi.z), az);
+    }
   });
   const float c = s.visc;
   return make_float3(c * ax, c * ay, c * az);
 }
 
-__global__ void __launch_bounds__(256) k_xsph_finalize(DeviceState d, const float4 *__restrict__ pred,
-                                                       const float4 *__restrict__ pos_in,
-                                                       float4 *__restrict__ pos_out, int keep_delta)
+// sph_velocity.glsl + sph_xsph.glsl + sph_finalize.glsl.
+template <bool EXACT>
+__global__ void __launch_bounds__(256) k_xsph_finalize_f(DeviceState d, const float4 *__restrict__ pred,
+                                                         const float4 *__restrict__ pos_in,
+                                                         float4 *__restrict__ pos_out, int keep_delta)
 {
   FLOWX_SLOT_PROLOGUE
   const float dtc = s.dtc;
+  const float inv_dtc = 1.0f / dtc;
   const float4 q = pred[i];
-  const float3 vi = slot_velocity(q, pos_in[i], dtc);
-  const float3 dv = xsph_sum(s, d.offsets, pred, d.lam, i, vi, [&](int k, const float4 &pj) {
-    return slot_velocity(pj, __ldg(&pos_in[k]), dtc);
+  const float4 p0 = pos_in[i];
+  float3 vi;
+  if (EXACT) {
+    vi = slot_velocity(q, p0, dtc);
+  } else {
+    vi = make_float3(__fmul_rn(__fsub_rn(q.x, p0.x), inv_dtc), __fmul_rn(__fsub_rn(q.y, p0.y), inv_dtc),
+                     __fmul_rn(__fsub_rn(q.z, p0.z), inv_dtc));
+  }
+  const float3 dv = xsph_sum_f<EXACT>(s, d, pred, i, q, vi, [&](int k, const float4 &pj) {
+    const float4 pk = __ldg(&pos_in[k]);
+    if (EXACT) return slot_velocity(pj, pk, dtc);
+    return make_float3(__fmul_rn(__fsub_rn(pj.x, pk.x), inv_dtc), __fmul_rn(__fsub_rn(pj.y, pk.y), inv_dtc),
+                       __fmul_rn(__fsub_rn(pj.z, pk.z), inv_dtc));
   });
   float3 v = make_float3(vi.x + dv.x, vi.y + dv.y, vi.z + dv.z);
   float3 p = make_float3(q.x, q.y, q.z);
@@ -105,29 +149,80 @@ __global__ void __launch_bounds__(256) k_xsph_finalize(DeviceState d, const floa
   if (keep_delta) d.delta[i] = make_float4(dv.x, dv.y, dv.z, 0.0f);
 }
 
-void launch_normal(const DeviceState &d, const float4 *pred, float4 *out, cudaStream_t st)
+// sph_normal.glsl:24-81 (over the previous substep's grid, as the reference).
+template <bool EXACT>
+__global__ void __launch_bounds__(256) k_normal_f(DeviceState d, const float4 *__restrict__ pred,
+                                                  float4 *__restrict__ out)
 {
-  const int b = blk(K_NORMAL, 128);
-  if (d.n > 0) k_normal<<<grid_for(d.n, b), b, 0, st>>>(d, pred, out);
-}
-void launch_lambda(const DeviceState &d, const float4 *pred, cudaStream_t st)
-{
-  const int b = blk(K_LAMBDA, 128);
-  if (d.n > 0) k_lambda<<<grid_for(d.n, b), b, 0, st>>>(d, pred);
-}
-void launch_delta_apply(const DeviceState &d, const float4 *pred_in, float4 *pred_out, cudaStream_t st)
-{
-  const int b = blk(K_DELTA_APPLY, 128);
-  if (d.n > 0) k_delta_apply<<<grid_for(d.n, b), b, 0, st>>>(d, pred_in, pred_out);
-}
-void launch_xsph_finalize(const DeviceState &d, const float4 *pred, const float4 *pos_in, float4 *pos_out,
-                          bool keep_delta, cudaStream_t st)
-{
-  const int b = blk(K_XSPH_FINALIZE, 128);
-  if (d.n > 0) k_xsph_finalize<<<grid_for(d.n, b), b, 0, st>>>(d, pred, pos_in, pos_out, keep_delta ? 1 : 0);
+  FLOWX_SLOT_PROLOGUE
+  const float4 pi = pred[i];
+  const int3 base = cell_coord(s, pi.x, pi.y, pi.z);
+  const float h = s.h, h2 = s.h2, mass = s.mass, poly6m6 = s.poly6m6, vlap = s.visclap;
+  float nx = 0.0f, ny = 0.0f, nz = 0.0f, lap = 0.0f;
+  for_each_within<EXACT>(s, d.offsets, pred, pi, h2, base, [&](int k) {
+    if (k == i) return;
+    const float4 pj = __ldg(&pred[k]);
+    const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+    const float r2 = pair_r2<EXACT>(dx, dy, dz);
+    if (r2 >= h2) return;
+    const float rho_j = fmaxf(__ldg(&d.lam[k].x), 1e-6f);
+    if (EXACT) {
+      const float weight = mass / rho_j;
+      const float t = h2 - r2;
+      const float sg = poly6m6 * t * t;
+      nx += weight * (sg * dx);
+      ny += weight * (sg * dy);
+      nz += weight * (sg * dz);
+      lap += weight * w_visc_lap(sqrtf(r2), h, vlap);
+    } else {
+      const float weight = __fdividef(mass, rho_j);
+      const float t = __fsub_rn(h2, r2);
+      const float sg = __fmul_rn(weight, __fmul_rn(poly6m6, __fmul_rn(t, t)));
+      nx = __fmaf_rn(sg, dx, nx);
+      ny = __fmaf_rn(sg, dy, ny);
+      nz = __fmaf_rn(sg, dz, nz);
+      // r = sqrt(r2); coincident particles (r2 = 0, e.g. two clamped into
+      // the same box corner) have r = 0, as sqrtf gives.
+      const float r = r2 > 0.0f ? __fmul_rn(r2, rsqrtf(r2)) : 0.0f;
+      lap = __fmaf_rn(__fmul_rn(weight, vlap), __fsub_rn(h, r), lap);
+    }
+  });
+  const float mag = sqrtf(nx * nx + ny * ny + nz * nz);
+  const float curv = (mag > 1e-4f) ? -lap / mag : 0.0f;
+  out[i] = make_float4(nx, ny, nz, curv);
 }
 
-// ---- single reference passes (per-pass API) ------------------------------
+void launch_lambda_f(const DeviceState &d, const float4 *pred, bool exact, cudaStream_t st)
+{
+  const int b = blk(K_LAMBDA, 128);
+  if (d.n <= 0) return;
+  if (exact) k_lambda_f<true><<<grid_for(d.n, b), b, 0, st>>>(d, pred);
+  else k_lambda_f<false><<<grid_for(d.n, b), b, 0, st>>>(d, pred);
+}
+void launch_delta_apply_f(const DeviceState &d, const float4 *pred_in, float4 *pred_out, bool exact, cudaStream_t st)
+{
+  const int b = blk(K_DELTA_APPLY, 128);
+  if (d.n <= 0) return;
+  if (exact) k_delta_apply_f<true><<<grid_for(d.n, b), b, 0, st>>>(d, pred_in, pred_out);
+  else k_delta_apply_f<false><<<grid_for(d.n, b), b, 0, st>>>(d, pred_in, pred_out);
+}
+void launch_xsph_finalize_f(const DeviceState &d, const float4 *pred, const float4 *pos_in, float4 *pos_out,
+                            bool keep_delta, bool exact, cudaStream_t st)
+{
+  const int b = blk(K_XSPH_FINALIZE, 128);
+  if (d.n <= 0) return;
+  if (exact) k_xsph_finalize_f<true><<<grid_for(d.n, b), b, 0, st>>>(d, pred, pos_in, pos_out, keep_delta);
+  else k_xsph_finalize_f<false><<<grid_for(d.n, b), b, 0, st>>>(d, pred, pos_in, pos_out, keep_delta);
+}
+void launch_normal_f(const DeviceState &d, const float4 *pred, float4 *out, bool exact, cudaStream_t st)
+{
+  const int b = blk(K_NORMAL, 128);
+  if (d.n <= 0) return;
+  if (exact) k_normal_f<true><<<grid_for(d.n, b), b, 0, st>>>(d, pred, out);
+  else k_normal_f<false><<<grid_for(d.n, b), b, 0, st>>>(d, pred, out);
+}
+
+// ---- single reference passes (per-pass API; always exact) ------------------
 // sph_predict.glsl:23-57
 __global__ void k_predict(DeviceState d, float4 *__restrict__ pred)
 {
@@ -142,7 +237,7 @@ __global__ void k_predict(DeviceState d, float4 *__restrict__ pred)
 __global__ void __launch_bounds__(256) k_delta(DeviceState d, const float4 *__restrict__ pred)
 {
   FLOWX_SLOT_PROLOGUE
-  const float3 a = delta_sum(s, d.offsets, pred, d.lam, i);
+  const float3 a = delta_sum_f<true>(s, d, pred, i, pred[i]);
   const float rest = s.rest;
   d.delta[i] = make_float4(a.x / rest, a.y / rest, a.z / rest, 0.0f);
 }
@@ -166,12 +261,12 @@ __global__ void __launch_bounds__(256) k_xsph(DeviceState d, const float4 *__res
 {
   FLOWX_SLOT_PROLOGUE
   const float4 vi4 = d.vel[i];
-  const float3 vi = make_float3(vi4.x, vi4.y, vi4.z);
   const float4 *__restrict__ vel = d.vel;
-  const float3 dv = xsph_sum(s, d.offsets, pred, d.lam, i, vi, [&](int k, const float4 &) {
-    const float4 v = __ldg(&vel[k]);
-    return make_float3(v.x, v.y, v.z);
-  });
+  const float3 dv = xsph_sum_f<true>(s, d, pred, i, pred[i], make_float3(vi4.x, vi4.y, vi4.z),
+                                     [&](int k, const float4 &) {
+                                       const float4 v = __ldg(&vel[k]);
+                                       return make_float3(v.x, v.y, v.z);
+                                     });
   d.delta[i] = make_float4(dv.x, dv.y, dv.z, 0.0f);
 }
 // sph_finalize.glsl:15-96
@@ -186,6 +281,11 @@ __global__ void k_finalize(DeviceState d, const float4 *__restrict__ pred)
   d.vel[i] = make_float4(v.x, v.y, v.z, 0.0f);
 }
 
+void launch_normal(const DeviceState &d, const float4 *pred, float4 *out, cudaStream_t st)
+{
+  launch_normal_f(d, pred, out, true, st);
+}
+void launch_lambda(const DeviceState &d, const float4 *pred, cudaStream_t st) { launch_lambda_f(d, pred, true, st); }
 void launch_predict(const DeviceState &d, float4 *pred, cudaStream_t st)
 {
   if (d.n > 0) k_predict<<<grid_for(d.n, 256), 256, 0, st>>>(d, pred);
@@ -213,7 +313,7 @@ void launch_finalize(const DeviceState &d, const float4 *pred, cudaStream_t st)
   if (d.n > 0) k_finalize<<<grid_for(d.n, 256), 256, 0, st>>>(d, pred);
 }
 
-// ---- per-frame density splat (surface_splat.glsl:32-97) -----------------
+// ---- per-frame density splat (surface_splat.glsl:32-97) -------------------
 // One thread per lattice sample of one segment's surface grid; gathers the
 // particles of the 5x5x5 cells around the sample's (clamped) cell.
 struct SplatParams {
@@ -275,7 +375,7 @@ void launch_splat_segment(const DeviceState &d, int seg, const float *surface_lo
   if (samples > 0) k_splat<<<grid_for(samples, b), b, 0, st>>>(d, sp, samples, out);
 }
 
-// ---- analytic collider voxeliser -----------------------------------------
+// ---- analytic collider voxeliser --------------------------------------------
 // Centre-inside occupancy of spheres, boxes and vertical cylinders, in double
 // precision, on the reference's collider-grid layout (origin at the domain's
 // low corner, x fastest: collision/__init__.py:245-254, :276-290).
@@ -300,13 +400,13 @@ __global__ void k_voxelize(uint8_t *__restrict__ grid, int nx, int ny, int nz, d
     const DevPrimitive p = prims[j];
     if (p.kind == 0) {
       const double dx = cx - p.a[0], dy = cy - p.a[1], dz = cz - p.a[2];
-      occ |= (dx * dx + dy * dy + dz * dz <= (double)p.r * p.r) ? 1 : 0;
+      occ |= (dx * dx + dy * dy + dz * dz <= p.r * p.r) ? 1 : 0;
     } else if (p.kind == 1) {
       occ |= (cx >= p.a[0] && cx <= p.b[0] && cy >= p.a[1] && cy <= p.b[1] && cz >= p.a[2] && cz <= p.b[2]) ? 1
                                                                                                            : 0;
     } else if (p.kind == 2) {
       const double dx = cx - p.a[0], dy = cy - p.a[1];
-      occ |= (dx * dx + dy * dy <= (double)p.r * p.r && cz >= p.a[2] && cz <= p.b[2]) ? 1 : 0;
+      occ |= (dx * dx + dy * dy <= p.r * p.r && cz >= p.a[2] && cz <= p.b[2]) ? 1 : 0;
     }
   }
   grid[t] = occ;

@@ -257,10 +257,12 @@ int Ctx::issue_substep(int iterations, int pred_in_idx)
 {
   float4 *pred_in = pred_in_idx == 0 ? d.pred_a : d.pred_b;
   const bool sigma = segs_need_normal();
+  const bool exact = (flags & FLOWX_FLAG_EXACT) != 0;
   // The substep's normals go to scratch in the old slot order; the permute
-  // moves them to the new order in the canonical buffer.
+  // moves them to the new order in the canonical buffer. The normal pass
+  // walks the previous substep's grid with that substep's masks.
   if (sigma) {
-    launch_normal(d, pred_in, d.normal_alt, stream);
+    launch_normal_f(d, pred_in, d.normal_alt, exact, stream);
     g_launches += 1;
   }
   launch_predict_key(d, d.normal_alt, stream);
@@ -271,12 +273,12 @@ int Ctx::issue_substep(int iterations, int pred_in_idx)
   g_launches += 8;
   float4 *q_in = d.pred_a, *q_out = d.pred_b;
   for (int it = 0; it < iterations; ++it) {
-    launch_lambda(d, q_in, stream);
-    launch_delta_apply(d, q_in, q_out, stream);
+    launch_lambda_f(d, q_in, exact, stream);
+    launch_delta_apply_f(d, q_in, q_out, exact, stream);
     g_launches += 2;
     std::swap(q_in, q_out);
   }
-  launch_xsph_finalize(d, q_in, d.pos_alt, d.pos, (flags & FLOWX_FLAG_KEEP_DELTA) != 0, stream);
+  launch_xsph_finalize_f(d, q_in, d.pos_alt, d.pos, (flags & FLOWX_FLAG_KEEP_DELTA) != 0, exact, stream);
   g_launches += 1;
   return FLOWX_OK;
 }
@@ -545,5 +547,6 @@ const char *flowx_kernel_name(int kernel_id)
 }
 
 int64_t flowx_launch_count(void) { return (int64_t)g_launches.load(); }
+
 
 }  // extern "C"

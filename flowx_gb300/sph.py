@@ -64,6 +64,7 @@ class Solver:
         max_surface_samples: int = 0,
         device: int = 0,
         keep_delta: bool = False,
+        exact: bool = False,
     ):
         self.lib = _lib.load()
         self.config = config
@@ -79,7 +80,7 @@ class Solver:
         cfg.max_collider_voxels = int(max_collider_voxels if max_collider_voxels is not None else vox)
         cfg.max_surface_samples = int(max_surface_samples)
         cfg.device = int(device)
-        cfg.flags = _lib.FLAG_KEEP_DELTA if keep_delta else 0
+        cfg.flags = (_lib.FLAG_KEEP_DELTA if keep_delta else 0) | (_lib.FLAG_EXACT if exact else 0)
         check(self.lib.flowx_create(ctypes.byref(cfg), ctypes.byref(self._ctx)))
         self.collider_dims = None
         self.collider_voxel = 0.0

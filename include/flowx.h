@@ -108,6 +108,12 @@ enum {
    * the reference's sph_xsph.glsl leaves it (off by default: nothing in the
    * substep reads it back). */
   FLOWX_FLAG_KEEP_DELTA = 1,
+  /* The fused substep evaluates the reference's float expressions operation
+   * for operation (bit-identical to a float32 evaluation without FMA
+   * contraction). Without it, pair terms are re-associated for throughput
+   * (FMA, one reciprocal square root per pair), within float32 rounding. The
+   * per-pass API (flowx_run_pass) is always exact. */
+  FLOWX_FLAG_EXACT = 2,
 };
 
 /* Sizes a context is created for (solver/sph.py:350-369 _allocate). */
