@@ -198,6 +198,68 @@ def _oracle_sample(scene, target_s=10.0, max_substeps=4):
     }
 
 
+def _batched_metrics(substeps=20, warmup=3):
+    """The 64-scene batched workload (particle counts log-uniform in
+    [2e3, 2e5]): one context stepping all scenes per launch, against the same
+    scenes stepped one after another, each in its own context with its own
+    CUDA graph. Both timed with CUDA events over ``substeps`` substeps after
+    ``warmup`` untimed ones."""
+    import torch
+
+    from flowx_gb300 import scenes
+    from flowx_gb300.batch import Batch
+    from flowx_gb300.sph import Solver
+
+    sc = scenes.batched_scenes()
+    total = sum(s.n for s in sc)
+    with Batch(sc) as b:
+        b.build_grid()
+        tuned = b.autotune(4)
+        for _ in range(warmup):
+            b.step(4, 1)
+        b.synchronize()
+        stream = torch.cuda.ExternalStream(b.stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(substeps):
+            b.step(4, 1)
+        e1.record(stream)
+        e1.synchronize()
+        batched_ms = e0.elapsed_time(e1)
+    solvers = [Solver(s.config, s.positions, s.velocities, collider=s.collider_grid(0), collider_voxel=s.collider_voxel)
+               for s in sc]
+    for s, sol in zip(sc, solvers):
+        sol._build_grid(0.0)
+        for _ in range(warmup):
+            sol.step_substeps(s.dt, 1)
+        sol.synchronize()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(substeps):
+        for s, sol in zip(sc, solvers):
+            sol.step_substeps(s.dt, 1)
+    for sol in solvers:
+        sol.synchronize()
+    seq_s = time.perf_counter() - t0
+    for sol in solvers:
+        sol.close()
+    batched = total * substeps / (batched_ms / 1e3)
+    sequential = total * substeps / seq_s
+    return {
+        "scenes": len(sc),
+        "particles": total,
+        "substeps": substeps,
+        "value": batched,
+        "sequential_value": sequential,
+        "unit": UNIT,
+        "speedup_vs_sequential": batched / sequential,
+        "ms_per_substep": batched_ms / substeps,
+        "autotuned_blocks": tuned,
+        "sequential": "each scene its own context and one-substep CUDA graph, issued one after another from one "
+                      "host thread (wall clock, synchronised at both ends)",
+    }
+
+
 def run_reference(args):
     """--impl reference: the reference's algorithm on the host cores."""
     world, rank, _ = _dist()
@@ -402,6 +464,10 @@ def run_flowx(args):
     finite = bool(np.isfinite(pinned_pos).all())
     sol.close()
 
+    batched = None
+    if not args.no_batched:
+        batched = _batched_metrics()
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         try:
@@ -432,6 +498,7 @@ def run_flowx(args):
             "clocks": clocks.summary(),
             "kernels": kernels,
             "math": "fast (re-associated float32; FLOWX_FLAG_EXACT gives the reference's expressions)",
+            "batched": batched,
             "splat_ms_per_frame": splat_ms,
             "splat_samples": samples,
             "state_finite": finite,
@@ -452,6 +519,7 @@ def main():
     ap.add_argument("--cell-rule", default="h", choices=["h", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 64-scene batched measurement")
     args = ap.parse_args()
     if args.warmup < 3:
         print("bench.py: --warmup below 3 is raised to 3", file=sys.stderr)

@@ -138,6 +138,16 @@ def load(path: str | None = None):
         "flowx_kernel_count": ([], ctypes.c_int),
         "flowx_kernel_name": ([ctypes.c_int], ctypes.c_char_p),
         "flowx_launch_count": ([], ctypes.c_int64),
+        "flowx_batch_set_scenes": ([ctx, P(Push), ctypes.c_int], ctypes.c_int),
+        "flowx_batch_scene_range": ([ctx, ctypes.c_int, P(ctypes.c_int32), P(ctypes.c_int32), P(ctypes.c_int32),
+                                     P(ctypes.c_int32)], ctypes.c_int),
+        "flowx_batch_set_collider": ([ctx, ctypes.c_int, vp, P(ctypes.c_int32), ctypes.c_float], ctypes.c_int),
+        "flowx_batch_build_grid": ([ctx], ctypes.c_int),
+        "flowx_batch_substep": ([ctx, ctypes.c_int], ctypes.c_int),
+        "flowx_batch_step": ([ctx, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+        "flowx_batch_splat": ([ctx, ctypes.c_int, P(Push), vp, ctypes.c_size_t], ctypes.c_int),
+        "flowx_autotune": ([ctx, P(Push), ctypes.c_int, P(ctypes.c_int32)], ctypes.c_int),
+        "flowx_set_block_sizes": ([ctx, P(ctypes.c_int32)], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

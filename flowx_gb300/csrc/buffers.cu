@@ -404,7 +404,17 @@ int flowx_profile_substeps(flowx_ctx *ctx, const flowx_push *push, int iteration
   if (rc) return rc;
   rc = c->ensure_offsets();
   if (rc) return rc;
-  rc = c->ensure_grid();
+  return c->profile_substeps(iterations, substeps, ms, launches);
+}
+
+}  // extern "C"
+
+// Fused substeps issued launch by launch with CUDA events around every
+// kernel; adds milliseconds and launch counts per kernel id.
+int Ctx::profile_substeps(int iterations, int substeps, float *ms, int32_t *launches)
+{
+  Ctx *c = this;
+  int rc = c->ensure_grid();
   if (rc) return rc;
   struct Rec {
     int kid, count;
@@ -458,5 +468,3 @@ int flowx_profile_substeps(flowx_ctx *ctx, const flowx_push *push, int iteration
   if (rc) return rc;
   return c->check_launch("flowx_profile_substeps");
 }
-
-}  // extern "C"

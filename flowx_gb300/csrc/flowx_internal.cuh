@@ -58,8 +58,51 @@ struct SegParams {
   long long s_begin;           // first sample of this segment in the output
 };
 
+// Kernels whose block size a context may choose (flowx_autotune).
+enum KernelId {
+  K_NORMAL = 0,
+  K_PREDICT_KEY,
+  K_SCAN_REDUCE,
+  K_SCAN_TOP,
+  K_SCAN_DOWN,
+  K_SCATTER,
+  K_CELL_SORT_SMALL,
+  K_CELL_SORT_LARGE,
+  K_PERMUTE_STEP,
+  K_LAMBDA,
+  K_DELTA_APPLY,
+  K_XSPH_FINALIZE,
+  K_SPLAT,
+  K_PREDICT,
+  K_DELTA,
+  K_APPLY,
+  K_VELOCITY,
+  K_XSPH,
+  K_FINALIZE,
+  K_PERMUTE_ALL,
+  K_GATHER,
+  K_SCATTER_IDS,
+  K_VOXELIZE,
+  K_COUNT
+};
+
+// Largest block a kernel can be launched with on the current device (its
+// register and shared-memory use; cached per kernel).
+int kernel_max_threads(const void *kernel);
+
+// Block size for a launch: the context's choice for the kernel (0 = `def`),
+// capped at what the kernel can launch with, in whole warps.
+#define FLOWX_BLOCK(d, kid, def, kernel)                                                   \
+  ([&]() {                                                                                  \
+    int b_ = (d).block[kid] > 0 ? (d).block[kid] : (def);                                   \
+    const int m_ = kernel_max_threads((const void *)(kernel));                              \
+    if (b_ > m_) b_ = m_ & ~31;                                                             \
+    return b_ < 32 ? 32 : b_;                                                               \
+  }())
+
 // Device pointers of one context's state (all in grid order).
 struct DeviceState {
+  int block[K_COUNT];       // block size per kernel, 0 = the kernel's default
   float4 *pos, *pos_alt;    // positions; pos_alt receives the permuted copy
   float4 *vel, *vel_alt;
   float4 *pred_a, *pred_b;  // predicted positions (Jacobi ping-pong)
@@ -183,34 +226,6 @@ __device__ __forceinline__ int3 collider_coord(const SegParams &s, float px, flo
 
 // ---- launch wrappers (defined in the kernel translation units) ------------
 // Block sizes are chosen per kernel by the tuner (runtime.cu); 0 = default.
-enum KernelId {
-  K_NORMAL = 0,
-  K_PREDICT_KEY,
-  K_SCAN_REDUCE,
-  K_SCAN_TOP,
-  K_SCAN_DOWN,
-  K_SCATTER,
-  K_CELL_SORT_SMALL,
-  K_CELL_SORT_LARGE,
-  K_PERMUTE_STEP,
-  K_LAMBDA,
-  K_DELTA_APPLY,
-  K_XSPH_FINALIZE,
-  K_SPLAT,
-  K_PREDICT,
-  K_DELTA,
-  K_APPLY,
-  K_VELOCITY,
-  K_XSPH,
-  K_FINALIZE,
-  K_PERMUTE_ALL,
-  K_GATHER,
-  K_SCATTER_IDS,
-  K_VOXELIZE,
-  K_COUNT
-};
-
-extern int g_block[K_COUNT];
 
 // grid build
 void launch_predict_key(const DeviceState &d, const float4 *normal_in, cudaStream_t st);

@@ -22,9 +22,8 @@
 
 namespace flowx {
 
-int g_block[K_COUNT] = {0};
 
-static inline int blk(KernelId k, int def) { return g_block[k] > 0 ? g_block[k] : def; }
+static inline int blk(const DeviceState &d, KernelId k, int def) { return d.block[k] > 0 ? d.block[k] : def; }
 static inline unsigned grid_for(long long n, int b) { return (unsigned)((n + b - 1) / b); }
 
 // ---- 1. predict + key + rank ---------------------------------------------
@@ -83,13 +82,13 @@ __global__ void k_key_only(DeviceState d, const float4 *__restrict__ pred)
 
 void launch_predict_key(const DeviceState &d, const float4 *normal_in, cudaStream_t st)
 {
-  const int b = blk(K_PREDICT_KEY, 256);
+  const int b = FLOWX_BLOCK(d, K_PREDICT_KEY, 256, k_predict_key);
   if (d.n > 0) k_predict_key<<<grid_for(d.n, b), b, 0, st>>>(d, normal_in);
 }
 
 void launch_key_only(const DeviceState &d, const float4 *pred, cudaStream_t st)
 {
-  const int b = blk(K_PREDICT_KEY, 256);
+  const int b = FLOWX_BLOCK(d, K_PREDICT_KEY, 256, k_key_only);
   if (d.n > 0) k_key_only<<<grid_for(d.n, b), b, 0, st>>>(d, pred);
 }
 
@@ -215,7 +214,7 @@ __global__ void k_scatter(DeviceState d)
 
 void launch_scatter(const DeviceState &d, cudaStream_t st)
 {
-  const int b = blk(K_SCATTER, 256);
+  const int b = FLOWX_BLOCK(d, K_SCATTER, 256, k_scatter);
   if (d.n > 0) k_scatter<<<grid_for(d.n, b), b, 0, st>>>(d);
 }
 
@@ -280,7 +279,7 @@ __global__ void __launch_bounds__(256) k_cell_sort_large(DeviceState d)
 
 void launch_cell_sort(const DeviceState &d, cudaStream_t st)
 {
-  const int b = blk(K_CELL_SORT_SMALL, 128);
+  const int b = FLOWX_BLOCK(d, K_CELL_SORT_SMALL, 128, k_cell_sort_small);
   if (d.cells > 0) k_cell_sort_small<<<grid_for(d.cells, b), b, 0, st>>>(d);
   k_cell_sort_large<<<d.sm_count, 256, 0, st>>>(d);
 }
@@ -312,7 +311,7 @@ __global__ void k_permute_step(DeviceState d, float4 *__restrict__ pred_out, con
 
 void launch_permute_step(const DeviceState &d, float4 *pred_out, const float4 *normal_in, cudaStream_t st)
 {
-  const int b = blk(K_PERMUTE_STEP, 256);
+  const int b = FLOWX_BLOCK(d, K_PERMUTE_STEP, 256, k_permute_step);
   if (d.n > 0) k_permute_step<<<grid_for(d.n, b), b, 0, st>>>(d, pred_out, normal_in);
 }
 
@@ -336,7 +335,7 @@ __global__ void k_permute_all(DeviceState d, const float4 *__restrict__ pred_in,
 
 void launch_permute_all(const DeviceState &d, const float4 *pred_in, float4 *pred_out, cudaStream_t st)
 {
-  const int b = blk(K_PERMUTE_ALL, 256);
+  const int b = FLOWX_BLOCK(d, K_PERMUTE_ALL, 256, k_permute_all);
   if (d.n > 0) k_permute_all<<<grid_for(d.n, b), b, 0, st>>>(d, pred_in, pred_out);
 }
 

@@ -19,7 +19,7 @@
 
 namespace flowx {
 
-static inline int blk(KernelId k, int def) { return g_block[k] > 0 ? g_block[k] : def; }
+static inline int blk(const DeviceState &d, KernelId k, int def) { return d.block[k] > 0 ? d.block[k] : def; }
 static inline unsigned grid_for(long long n, int b) { return (unsigned)((n + b - 1) / b); }
 
 #define FLOWX_SLOT_PROLOGUE                            \
@@ -37,7 +37,7 @@ __device__ __forceinline__ float3 slot_velocity(const float4 &q, const float4 &p
 
 // sph_lambda.glsl:17-77
 template <bool EXACT>
-__global__ void __launch_bounds__(256) k_lambda_f(DeviceState d, const float4 *__restrict__ pred)
+__global__ void __launch_bounds__(512) k_lambda_f(DeviceState d, const float4 *__restrict__ pred)
 {
   FLOWX_SLOT_PROLOGUE
   const float4 pi = pred[i];
@@ -72,7 +72,7 @@ __device__ __forceinline__ float3 delta_sum_f(const SegParams &s, const DeviceSt
 
 // sph_delta.glsl + sph_apply_delta.glsl: pred_out = pred_in + sum / rho0.
 template <bool EXACT>
-__global__ void __launch_bounds__(256) k_delta_apply_f(DeviceState d, const float4 *__restrict__ pred_in,
+__global__ void __launch_bounds__(512) k_delta_apply_f(DeviceState d, const float4 *__restrict__ pred_in,
                                                        float4 *__restrict__ pred_out)
 {
   FLOWX_SLOT_PROLOGUE
@@ -119,7 +119,7 @@ __device__ __forceinline__ float3 xsph_sum_f(const SegParams &s, const DeviceSta
 
 // sph_velocity.glsl + sph_xsph.glsl + sph_finalize.glsl.
 template <bool EXACT>
-__global__ void __launch_bounds__(256) k_xsph_finalize_f(DeviceState d, const float4 *__restrict__ pred,
+__global__ void __launch_bounds__(512) k_xsph_finalize_f(DeviceState d, const float4 *__restrict__ pred,
                                                          const float4 *__restrict__ pos_in,
                                                          float4 *__restrict__ pos_out, int keep_delta)
 {
@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(256) k_xsph_finalize_f(DeviceState d, const fl
 
 // sph_normal.glsl:24-81 (over the previous substep's grid, as the reference).
 template <bool EXACT>
-__global__ void __launch_bounds__(256) k_normal_f(DeviceState d, const float4 *__restrict__ pred,
+__global__ void __launch_bounds__(512) k_normal_f(DeviceState d, const float4 *__restrict__ pred,
                                                   float4 *__restrict__ out)
 {
   FLOWX_SLOT_PROLOGUE
@@ -194,14 +194,15 @@ __global__ void __launch_bounds__(256) k_normal_f(DeviceState d, const float4 *_
 
 void launch_lambda_f(const DeviceState &d, const float4 *pred, bool exact, cudaStream_t st)
 {
-  const int b = blk(K_LAMBDA, 128);
+  const int b = FLOWX_BLOCK(d, K_LAMBDA, 128, exact ? (const void *)k_lambda_f<true> : (const void *)k_lambda_f<false>);
   if (d.n <= 0) return;
   if (exact) k_lambda_f<true><<<grid_for(d.n, b), b, 0, st>>>(d, pred);
   else k_lambda_f<false><<<grid_for(d.n, b), b, 0, st>>>(d, pred);
 }
 void launch_delta_apply_f(const DeviceState &d, const float4 *pred_in, float4 *pred_out, bool exact, cudaStream_t st)
 {
-  const int b = blk(K_DELTA_APPLY, 128);
+  const int b = FLOWX_BLOCK(d, K_DELTA_APPLY, 128,
+                            exact ? (const void *)k_delta_apply_f<true> : (const void *)k_delta_apply_f<false>);
   if (d.n <= 0) return;
   if (exact) k_delta_apply_f<true><<<grid_for(d.n, b), b, 0, st>>>(d, pred_in, pred_out);
   else k_delta_apply_f<false><<<grid_for(d.n, b), b, 0, st>>>(d, pred_in, pred_out);
@@ -209,14 +210,15 @@ void launch_delta_apply_f(const DeviceState &d, const float4 *pred_in, float4 *p
 void launch_xsph_finalize_f(const DeviceState &d, const float4 *pred, const float4 *pos_in, float4 *pos_out,
                             bool keep_delta, bool exact, cudaStream_t st)
 {
-  const int b = blk(K_XSPH_FINALIZE, 128);
+  const int b = FLOWX_BLOCK(d, K_XSPH_FINALIZE, 128,
+                            exact ? (const void *)k_xsph_finalize_f<true> : (const void *)k_xsph_finalize_f<false>);
   if (d.n <= 0) return;
   if (exact) k_xsph_finalize_f<true><<<grid_for(d.n, b), b, 0, st>>>(d, pred, pos_in, pos_out, keep_delta);
   else k_xsph_finalize_f<false><<<grid_for(d.n, b), b, 0, st>>>(d, pred, pos_in, pos_out, keep_delta);
 }
 void launch_normal_f(const DeviceState &d, const float4 *pred, float4 *out, bool exact, cudaStream_t st)
 {
-  const int b = blk(K_NORMAL, 128);
+  const int b = FLOWX_BLOCK(d, K_NORMAL, 128, exact ? (const void *)k_normal_f<true> : (const void *)k_normal_f<false>);
   if (d.n <= 0) return;
   if (exact) k_normal_f<true><<<grid_for(d.n, b), b, 0, st>>>(d, pred, out);
   else k_normal_f<false><<<grid_for(d.n, b), b, 0, st>>>(d, pred, out);
@@ -234,7 +236,7 @@ __global__ void k_predict(DeviceState d, float4 *__restrict__ pred)
   pred[i] = make_float4(q.x, q.y, q.z, 1.0f);
 }
 // sph_delta.glsl:19-85
-__global__ void __launch_bounds__(256) k_delta(DeviceState d, const float4 *__restrict__ pred)
+__global__ void __launch_bounds__(512) k_delta(DeviceState d, const float4 *__restrict__ pred)
 {
   FLOWX_SLOT_PROLOGUE
   const float3 a = delta_sum_f<true>(s, d, pred, i, pred[i]);
@@ -257,7 +259,7 @@ __global__ void k_velocity(DeviceState d, const float4 *__restrict__ pred)
   d.vel[i] = make_float4(v.x, v.y, v.z, 0.0f);
 }
 // sph_xsph.glsl:28-82
-__global__ void __launch_bounds__(256) k_xsph(DeviceState d, const float4 *__restrict__ pred)
+__global__ void __launch_bounds__(512) k_xsph(DeviceState d, const float4 *__restrict__ pred)
 {
   FLOWX_SLOT_PROLOGUE
   const float4 vi4 = d.vel[i];
@@ -292,7 +294,7 @@ void launch_predict(const DeviceState &d, float4 *pred, cudaStream_t st)
 }
 void launch_delta(const DeviceState &d, const float4 *pred, cudaStream_t st)
 {
-  const int b = blk(K_DELTA, 128);
+  const int b = FLOWX_BLOCK(d, K_DELTA, 128, k_delta);
   if (d.n > 0) k_delta<<<grid_for(d.n, b), b, 0, st>>>(d, pred);
 }
 void launch_apply(const DeviceState &d, float4 *pred, cudaStream_t st)
@@ -305,7 +307,7 @@ void launch_velocity(const DeviceState &d, const float4 *pred, cudaStream_t st)
 }
 void launch_xsph(const DeviceState &d, const float4 *pred, cudaStream_t st)
 {
-  const int b = blk(K_XSPH, 128);
+  const int b = FLOWX_BLOCK(d, K_XSPH, 128, k_xsph);
   if (d.n > 0) k_xsph<<<grid_for(d.n, b), b, 0, st>>>(d, pred);
 }
 void launch_finalize(const DeviceState &d, const float4 *pred, cudaStream_t st)
@@ -323,7 +325,7 @@ struct SplatParams {
   int seg;
 };
 
-__global__ void __launch_bounds__(256) k_splat(DeviceState d, SplatParams sp, long long samples,
+__global__ void __launch_bounds__(512) k_splat(DeviceState d, SplatParams sp, long long samples,
                                                float *__restrict__ out)
 {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -371,7 +373,7 @@ void launch_splat_segment(const DeviceState &d, int seg, const float *surface_lo
   sp.snz = dims[2];
   sp.seg = seg;
   const long long samples = (long long)dims[0] * dims[1] * dims[2];
-  const int b = blk(K_SPLAT, 128);
+  const int b = FLOWX_BLOCK(d, K_SPLAT, 128, k_splat);
   if (samples > 0) k_splat<<<grid_for(samples, b), b, 0, st>>>(d, sp, samples, out);
 }
 

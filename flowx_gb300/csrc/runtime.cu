@@ -13,6 +13,7 @@
 #include <tuple>
 #include <vector>
 #include <atomic>
+#include <mutex>
 
 #include "../../include/flowx.h"
 #include "flowx_internal.cuh"
@@ -31,6 +32,23 @@ static const char *kKernelNames[K_COUNT] = {
     "splat",         "predict",      "delta",       "apply_delta",  "velocity",     "xsph",
     "finalize",      "permute_all",  "gather",      "scatter_ids",  "voxelize",
 };
+
+int kernel_max_threads(const void *kernel)
+{
+  static std::mutex mu;
+  static std::map<std::pair<int, const void *>, int> cache;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lock(mu);
+  auto key = std::make_pair(dev, kernel);
+  auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
+  cudaFuncAttributes attr{};
+  int m = 1024;
+  if (cudaFuncGetAttributes(&attr, kernel) == cudaSuccess) m = attr.maxThreadsPerBlock;
+  cache[key] = m;
+  return m;
+}
 
 float bits_to_float(int32_t b)
 {
@@ -169,11 +187,18 @@ void Ctx::release()
 
 float4 *Ctx::pred_cur() { return pred_idx == 0 ? d.pred_a : d.pred_b; }
 
+// Captured graphs bake in launch shapes; drop them when those change.
+void Ctx::drop_graphs()
+{
+  for (auto &kv : graphs) cudaGraphExecDestroy(kv.second.exec);
+  graphs.clear();
+}
+
 // Resolve and upload the segment table for a push (single-scene contexts).
 int Ctx::set_push(const flowx_push *push)
 {
   if (!push) return fail(FLOWX_ERR_ARG, "push block is NULL");
-  if (segs.size() != 1) return fail(FLOWX_ERR_STATE, "batched context: use the flowx_batch_* entry points");
+  if (batch) return fail(FLOWX_ERR_STATE, "batched context: use the flowx_batch_* entry points");
   if (push->i_layout[0] != total_particles)
     return fail(FLOWX_ERR_ARG, "push i_layout.x (particle count " + std::to_string(push->i_layout[0]) +
                                    ") differs from the context's " + std::to_string(total_particles));
@@ -202,12 +227,26 @@ int Ctx::upload_segs(const std::vector<SegParams> &s, int cells)
 {
   const bool same = s.size() == segs.size() && std::memcmp(s.data(), segs.data(), s.size() * sizeof(SegParams)) == 0;
   if (!same || !segs_uploaded) {
+    if (s.size() > seg_capacity) {
+      // A batch with more scenes than the table holds: grow it (stream work
+      // that may still read the old table is finished first).
+      int rc = cuda(cudaStreamSynchronize(stream), "segment table resize");
+      if (rc) return rc;
+      if (d_segs) cudaFree(d_segs);
+      d_segs = nullptr;
+      rc = cuda(cudaMalloc((void **)&d_segs, s.size() * sizeof(SegParams)), "segment table allocation");
+      if (rc) return rc;
+      seg_capacity = s.size();
+      drop_graphs();
+    }
     segs = s;
     int rc = cuda(cudaMemcpyAsync(d_segs, segs.data(), segs.size() * sizeof(SegParams), cudaMemcpyHostToDevice,
                                   stream),
                   "segment table upload");
     if (rc) return rc;
     segs_uploaded = true;
+    d.segs = d_segs;
+    d.nseg = (int)segs.size();
   }
   if (cells != d.cells) {
     if (have_grid && cells != d.cells) have_grid = false;

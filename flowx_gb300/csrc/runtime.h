@@ -40,6 +40,7 @@ struct Ctx {
   int prim_cap = 0;
   std::vector<SegParams> segs;
   bool segs_uploaded = false;
+  size_t seg_capacity = 1;         // entries the device segment table holds
   int pred_idx = 0;                // predicted positions live in pred_a (0) or pred_b (1)
   bool have_grid = false;          // keys / ids / offsets describe a built grid
   bool offsets_dirty = false;      // keys were uploaded; offsets follow on the next push
@@ -73,6 +74,12 @@ struct Ctx {
   int substep(int iterations);
   int step(int iterations, int substeps);
   int reorder_state(const std::vector<uint32_t> &src_slot);
+  int profile_substeps(int iterations, int substeps, float *ms, int32_t *launches);
+  // batched scenes
+  bool batch = false;
+  std::vector<long long> scene_voxels;  // collider voxels of each scene (0 = none)
+  std::vector<char> scene_collider;     // collider installed per scene
+  void drop_graphs();
 };
 
 }  // namespace flowx

@@ -223,6 +223,48 @@ const char *flowx_kernel_name(int kernel_id);
 /* Total number of kernel launches this library has issued (all contexts). */
 int64_t flowx_launch_count(void);
 
+/* ---- batched scenes -------------------------------------------------------
+ * No reference counterpart: the reference simulates one domain per scene
+ * (README.md:141). A batch is a context created for the summed particle,
+ * cell and collider-voxel counts of several independent scenes; every kernel
+ * of the substep then serves all scenes in one launch. Particle buffers
+ * (flowx_upload / flowx_download) are the scenes' arrays concatenated in scene
+ * order; downloaded keys carry the batch-global cell index. */
+
+/* Install the scenes, one push block each (particle count, grid, parameters,
+ * collider dims / voxel). The counts must sum to the context's particle
+ * count. Single-scene entry points (flowx_substep, flowx_step, ...) are then
+ * refused; use the batch ones. */
+int flowx_batch_set_scenes(flowx_ctx *ctx, const flowx_push *pushes, int nscenes);
+
+/* Where a scene lives in the concatenated arrays. */
+int flowx_batch_scene_range(flowx_ctx *ctx, int scene, int32_t *first_particle, int32_t *particle_count,
+                            int32_t *first_cell, int32_t *cell_count);
+
+/* Collider occupancy of one scene (layout of flowx_set_collider); dims and
+ * voxel must match the scene's push block. */
+int flowx_batch_set_collider(flowx_ctx *ctx, int scene, const uint8_t *occupancy, const int32_t dims[3],
+                             float voxel_size);
+
+/* Grid build, one substep, or `substeps` substeps as one CUDA-graph launch,
+ * for all scenes at once (each with its own dt and parameters). */
+int flowx_batch_build_grid(flowx_ctx *ctx);
+int flowx_batch_substep(flowx_ctx *ctx, int iterations);
+int flowx_batch_step(flowx_ctx *ctx, int iterations, int substeps);
+
+/* The density splat of one scene, with that scene's splat push block. */
+int flowx_batch_splat(flowx_ctx *ctx, int scene, const flowx_push *splat_push, float *host_out, size_t bytes);
+
+/* ---- launch shapes ----------------------------------------------------------
+ * Block sizes per kernel: flowx_autotune times the fused substep launch by
+ * launch with candidate sizes (64, 128, 256, 512) on the context's current
+ * state, restoring that state after every trial, and keeps the fastest per
+ * kernel; chosen (flowx_kernel_count() entries, may be NULL) receives the
+ * result, 0 meaning the kernel's default. `push` is ignored for a batch.
+ * flowx_set_block_sizes installs sizes directly. No reference counterpart. */
+int flowx_autotune(flowx_ctx *ctx, const flowx_push *push, int iterations, int32_t *chosen);
+int flowx_set_block_sizes(flowx_ctx *ctx, const int32_t *blocks);
+
 #ifdef __cplusplus
 }
 #endif
