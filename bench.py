@@ -400,7 +400,7 @@ def run_flowx(args):
     traffic_path = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(traffic_path):
         with open(traffic_path) as f:
-            traffic = json.load(f).get(dominant)
+            traffic = json.load(f).get("bytes_per_launch", {}).get(dominant)
     roofline = {
         "bound": "hbm",
         "kernel": dominant,
@@ -520,13 +520,46 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-scene batched measurement")
+    ap.add_argument("--case", action="store_true",
+                    help="untimed launch-by-launch run of --warmup frames, for profiler captures")
+    ap.add_argument("--exact", action="store_true", help="with --case: the reference's float expressions")
     args = ap.parse_args()
     if args.warmup < 3:
         print("bench.py: --warmup below 3 is raised to 3", file=sys.stderr)
         args.warmup = 3
+    if args.case:
+        return run_case(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_flowx(args)
+
+
+def run_case(args):
+    """Untimed run for profiler captures: seed the workload, build the grid,
+    run --warmup frames launch by launch (no CUDA graph, so every kernel is a
+    separate launch), check the state is finite and exit."""
+    import torch
+
+    from flowx_gb300.sph import Solver
+
+    torch.cuda.set_device(0)
+    scene = _workload(args)
+    c = scene.config
+    sol = Solver(c, scene.positions, scene.velocities, max_cells=c.cell_count,
+                 max_collider_voxels=int(np.prod(scene.collider_dims)) if scene.collider_dims else 0,
+                 exact=args.exact)
+    if scene.collider_dims is not None:
+        sol.voxelize(scene.primitives_at(0), scene.collider_dims, scene.collider_voxel)
+    sol._build_grid(0.0)
+    for f in range(args.warmup):
+        if scene.collider_dims is not None:
+            sol.voxelize(scene.primitives_at(f), scene.collider_dims, scene.collider_voxel)
+        for _ in range(scene.substeps_per_frame):
+            sol._substep(scene.dt)
+    ok = bool(np.isfinite(sol.read("positions")).all())
+    sol.close()
+    print(json.dumps({"case": scene.name, "frames": args.warmup, "finite": ok}))
+    return 0 if ok else 1
 
 
 if __name__ == "__main__":
