@@ -148,6 +148,8 @@ def load(path: str | None = None):
         "flowx_batch_splat": ([ctx, ctypes.c_int, P(Push), vp, ctypes.c_size_t], ctypes.c_int),
         "flowx_autotune": ([ctx, P(Push), ctypes.c_int, P(ctypes.c_int32)], ctypes.c_int),
         "flowx_set_block_sizes": ([ctx, P(ctypes.c_int32)], ctypes.c_int),
+        "flowx_build_grid_static": ([vp, ctypes.c_int32, P(Push), vp, ctypes.c_int32, vp, vp, vp], ctypes.c_int),
+        "flowx_build_grid_static_error": ([], ctypes.c_char_p),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -265,6 +265,36 @@ int flowx_batch_splat(flowx_ctx *ctx, int scene, const flowx_push *splat_push, f
 int flowx_autotune(flowx_ctx *ctx, const flowx_push *push, int iterations, int32_t *chosen);
 int flowx_set_block_sizes(flowx_ctx *ctx, const int32_t *blocks);
 
+/* Grid build that allocates nothing. There is no counterpart in the
+ * reference: its grid build (solver/sph.py:482-498) always runs inside a
+ * context that owns its buffers.
+ *
+ * For callers that cannot let a library allocate device memory: an
+ * application that reserves its device-memory budget up front and hands out
+ * pieces of it, or code in a region where the device-wide synchronisation of
+ * cudaMalloc / cudaFree is not allowed. No context: all arguments are device
+ * pointers owned by the caller.
+ *   predicted    particle_count x float4, predicted positions in id order
+ *   keys         key_count x float4 out, key_count >= particle_count; the KEYS
+ *                layout above (padding slots get (cell count, slot))
+ *   cell_start,  C x float out each, C = push->i_grid[3]; -1 for an empty
+ *   cell_end     cell (the CELL_START / CELL_END layouts above)
+ *   stream       cudaStream_t the work is ordered on (NULL = default stream)
+ * The result equals flowx_build_grid's for the same predicted positions and
+ * push block. Returns without waiting for the GPU.
+ *
+ * Scratch is one static device array of the library, sized for at most
+ * 65536 particles and 262144 cells; larger sizes return FLOWX_ERR_CAPACITY.
+ * The first call made with a device current looks the array's address up
+ * for that device: make it before any stream capture. Every call clears the
+ * cell counters (the only scratch that must start at zero) itself. All calls
+ * on a device share the scratch, so calls whose GPU work overlaps (different
+ * streams or host threads) race: order them on one stream. The message of
+ * a failure is returned by flowx_build_grid_static_error (per host thread). */
+int flowx_build_grid_static(const float *predicted, int32_t particle_count, const flowx_push *push, float *keys,
+                            int32_t key_count, float *cell_start, float *cell_end, void *stream);
+const char *flowx_build_grid_static_error(void);
+
 #ifdef __cplusplus
 }
 #endif
