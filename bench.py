@@ -46,6 +46,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "PBF particle-substeps/s (4M particles, 4 Jacobi iterations)"
 UNIT = "particle-substeps/s"
+ADJOINT_SUBSTEPS = 30  # the inverse problem's rollout
 
 # Algorithmic bytes per particle and launch of each kernel (compulsory HBM
 # traffic: every array touched once per launch, neighbour reuse served on chip;
@@ -260,6 +261,59 @@ def _batched_metrics(substeps=20, warmup=3):
     }
 
 
+def _adjoint_metrics(adam_steps=200, repeats=5):
+    """The differentiable workload (20,000 particles in a 1 m cube, h 0.04,
+    initial velocities from a 3x3x3 control grid of 3-vectors, loss = squared
+    L2 distance of the 64^3 splat after 30 substeps x 4 iterations to the
+    splat of a hidden control grid). Forward and forward+adjoint wall time per
+    substep through the autograd.Function (each call synchronises the
+    library's stream), then ``adam_steps`` Adam steps on the control grid,
+    and the same optimiser over a 3-substep rollout for comparison."""
+    import torch
+
+    from flowx_gb300 import scenes
+    from flowx_gb300.adjoint import InverseProblem
+
+    ip = InverseProblem(scenes.inverse_problem(), substeps=ADJOINT_SUBSTEPS)
+    control = ip.initial.clone().requires_grad_(True)
+    for _ in range(3):
+        control.grad = None
+        ip.loss(control).backward()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(repeats):
+        with torch.no_grad():
+            ip.loss(control)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for _ in range(repeats):
+        control.grad = None
+        ip.loss(control).backward()
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    fwd = (t1 - t0) / repeats / ADJOINT_SUBSTEPS * 1e3
+    both = (t2 - t1) / repeats / ADJOINT_SUBSTEPS * 1e3
+    grad_norm = float(control.grad.norm())
+    t3 = time.perf_counter()
+    losses, _ = ip.optimise(steps=adam_steps, lr=0.05)
+    adam_s = time.perf_counter() - t3
+    short = InverseProblem(scenes.inverse_problem(), substeps=3)
+    short_losses, _ = short.optimise(steps=adam_steps, lr=0.05)
+    return {
+        "workload": f"inverse problem: {ip.solver.n} particles, {ADJOINT_SUBSTEPS} substeps x 4 iterations, "
+                    "64^3 splat, 3x3x3x3 control grid",
+        "fwd_ms_per_substep": fwd,
+        "fwd_adjoint_ms_per_substep": both,
+        "fwd_adjoint_over_fwd": both / fwd,
+        "timing": "wall clock around the autograd.Function call, synchronised at both ends",
+        "control_gradient_norm": grad_norm,
+        "adam": {"steps": adam_steps, "lr": 0.05, "loss_first": losses[0], "loss_min": min(losses),
+                 "loss_min_step": int(np.argmin(losses)), "loss_last": losses[-1], "seconds": adam_s},
+        "adam_3_substeps": {"steps": adam_steps, "lr": 0.05, "loss_first": short_losses[0],
+                            "loss_last": short_losses[-1]},
+    }
+
+
 def run_reference(args):
     """--impl reference: the reference's algorithm on the host cores."""
     world, rank, _ = _dist()
@@ -467,6 +521,9 @@ def run_flowx(args):
     batched = None
     if not args.no_batched:
         batched = _batched_metrics()
+    adjoint = None
+    if rank == 0 and not args.no_adjoint:
+        adjoint = _adjoint_metrics()
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -499,6 +556,7 @@ def run_flowx(args):
             "kernels": kernels,
             "math": "fast (re-associated float32; FLOWX_FLAG_EXACT gives the reference's expressions)",
             "batched": batched,
+            "adjoint": adjoint,
             "splat_ms_per_frame": splat_ms,
             "splat_samples": samples,
             "state_finite": finite,
@@ -515,11 +573,13 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["flowx", "reference"], default="flowx")
-    ap.add_argument("--workload", default="large", choices=["large", "pool", "dam_break"])
+    ap.add_argument("--workload", default="large", choices=["large", "pool", "dam_break", "inverse"],
+                    help="inverse (the differentiable 20,000-particle problem) is a --case workload only")
     ap.add_argument("--cell-rule", default="h", choices=["h", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-scene batched measurement")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-substep measurement")
     ap.add_argument("--case", action="store_true",
                     help="untimed launch-by-launch run of --warmup frames, for profiler captures")
     ap.add_argument("--exact", action="store_true", help="with --case: the reference's float expressions")
@@ -528,7 +588,9 @@ def main():
         print("bench.py: --warmup below 3 is raised to 3", file=sys.stderr)
         args.warmup = 3
     if args.case:
-        return run_case(args)
+        return run_case_adjoint(args) if args.workload == "inverse" else run_case(args)
+    if args.workload == "inverse":
+        raise SystemExit("--workload inverse is a --case workload; the bench line reports it under 'adjoint'")
     if args.impl == "reference":
         return run_reference(args)
     return run_flowx(args)
@@ -559,6 +621,24 @@ def run_case(args):
     ok = bool(np.isfinite(sol.read("positions")).all())
     sol.close()
     print(json.dumps({"case": scene.name, "frames": args.warmup, "finite": ok}))
+    return 0 if ok else 1
+
+
+def run_case_adjoint(args):
+    """Untimed run for profiler captures of the differentiable substeps: the
+    inverse problem's target forward, then one forward and one adjoint."""
+    import torch
+
+    from flowx_gb300 import scenes
+    from flowx_gb300.adjoint import InverseProblem
+
+    torch.cuda.set_device(0)
+    ip = InverseProblem(scenes.inverse_problem(), substeps=ADJOINT_SUBSTEPS)
+    control = ip.initial.clone().requires_grad_(True)
+    loss = ip.loss(control)
+    loss.backward()
+    ok = bool(torch.isfinite(control.grad).all()) and bool(torch.isfinite(loss))
+    print(json.dumps({"case": "inverse", "substeps": ADJOINT_SUBSTEPS, "finite": ok}))
     return 0 if ok else 1
 
 

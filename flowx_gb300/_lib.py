@@ -91,6 +91,21 @@ class Primitive(ctypes.Structure):
     ]
 
 
+class AdjointConfig(ctypes.Structure):
+    """flowx_adjoint_config (include/flowx.h)."""
+
+    _fields_ = [
+        ("particle_count", ctypes.c_int32),
+        ("max_cells", ctypes.c_int32),
+        ("max_substeps", ctypes.c_int32),
+        ("max_iterations", ctypes.c_int32),
+        ("max_collider_voxels", ctypes.c_int64),
+        ("max_surface_samples", ctypes.c_int64),
+        ("device", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+    ]
+
+
 class FlowxError(RuntimeError):
     def __init__(self, code, message):
         super().__init__(f"{ERRORS.get(code, code)}: {message}")
@@ -148,6 +163,14 @@ def load(path: str | None = None):
         "flowx_batch_splat": ([ctx, ctypes.c_int, P(Push), vp, ctypes.c_size_t], ctypes.c_int),
         "flowx_autotune": ([ctx, P(Push), ctypes.c_int, P(ctypes.c_int32)], ctypes.c_int),
         "flowx_set_block_sizes": ([ctx, P(ctypes.c_int32)], ctypes.c_int),
+        "flowx_adjoint_create": ([P(AdjointConfig), P(vp)], ctypes.c_int),
+        "flowx_adjoint_destroy": ([vp], ctypes.c_int),
+        "flowx_adjoint_last_error": ([vp], ctypes.c_char_p),
+        "flowx_adjoint_get_stream": ([vp, P(vp)], ctypes.c_int),
+        "flowx_adjoint_set_collider": ([vp, vp, P(ctypes.c_int32), ctypes.c_float], ctypes.c_int),
+        "flowx_adjoint_forward": ([vp, P(Push), ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, P(Push), vp],
+                                  ctypes.c_int),
+        "flowx_substep_adjoint": ([vp, vp, vp, vp, vp, vp], ctypes.c_int),
         "flowx_build_grid_static": ([vp, ctypes.c_int32, P(Push), vp, ctypes.c_int32, vp, vp, vp], ctypes.c_int),
         "flowx_build_grid_static_error": ([], ctypes.c_char_p),
     }

@@ -265,6 +265,48 @@ int flowx_batch_splat(flowx_ctx *ctx, int scene, const flowx_push *splat_push, f
 int flowx_autotune(flowx_ctx *ctx, const flowx_push *push, int iterations, int32_t *chosen);
 int flowx_set_block_sizes(flowx_ctx *ctx, const int32_t *blocks);
 
+/* ---- Differentiable substeps (no reference counterpart) -------------------
+ * A checkpointed forward of the fused substep (solver/sph.py:501-514, the
+ * same float32 expressions as FLOWX_FLAG_EXACT) and its hand-written adjoint.
+ * Particle arrays here are DEVICE pointers (N x float4, particle-id order) on
+ * the object's stream. The neighbour grid of every substep is held fixed
+ * (not differentiated); the state entering each substep is checkpointed and
+ * the Jacobi iterates are recomputed during the adjoint. The first substep
+ * sees the state the reference's _allocate and _seed leave (sph.py:350-369,
+ * :606): predicted = positions, densities zero, grid built from positions. */
+typedef struct flowx_adjoint flowx_adjoint;
+
+typedef struct flowx_adjoint_config {
+  int32_t particle_count;
+  int32_t max_cells;
+  int32_t max_substeps;        /* substeps one forward may record */
+  int32_t max_iterations;      /* Jacobi iterations per substep, >= 1 */
+  int64_t max_collider_voxels;
+  int64_t max_surface_samples; /* splat grid capacity, 0 = no splat */
+  int32_t device;
+  int32_t reserved;
+} flowx_adjoint_config;
+
+int flowx_adjoint_create(const flowx_adjoint_config *config, flowx_adjoint **out);
+int flowx_adjoint_destroy(flowx_adjoint *adj);
+const char *flowx_adjoint_last_error(const flowx_adjoint *adj);
+int flowx_adjoint_get_stream(flowx_adjoint *adj, void **stream);
+/* Collider occupancy (host bytes, the flowx_set_collider layout). */
+int flowx_adjoint_set_collider(flowx_adjoint *adj, const uint8_t *occupancy, const int32_t dims[3], float voxel_size);
+/* `substeps` substeps with `iterations` Jacobi iterations from (positions,
+ * velocities); writes the final state to positions_out / velocities_out and,
+ * when splat_push is not NULL, the density splat of the final positions
+ * (flowx_splat's values) to surface. Records what flowx_substep_adjoint needs. */
+int flowx_adjoint_forward(flowx_adjoint *adj, const flowx_push *push, int iterations, int substeps,
+                          const float *positions, const float *velocities, float *positions_out,
+                          float *velocities_out, const flowx_push *splat_push, float *surface);
+/* Reverse mode over the substeps of the last flowx_adjoint_forward: given the
+ * cotangents of the surface (NULL = zero), the final positions and the final
+ * velocities (NULL = zero), writes the gradients with respect to the initial
+ * positions and velocities (N x float4 each, w lanes zero). */
+int flowx_substep_adjoint(flowx_adjoint *adj, const float *surface_grad, const float *positions_out_grad,
+                          const float *velocities_out_grad, float *positions_grad, float *velocities_grad);
+
 /* Grid build that allocates nothing. There is no counterpart in the
  * reference: its grid build (solver/sph.py:482-498) always runs inside a
  * context that owns its buffers.
