@@ -82,6 +82,75 @@ __device__ __forceinline__ float3 jphi(float3 d, float r, float h, float3 y)
   return sub3(scale3(y, a), scale3(d, b * dot3(d, y)));
 }
 
+// ---- warp-per-particle neighbour walks ---------------------------------------
+// At the sizes this path serves (tens of thousands of particles) one thread
+// per particle leaves the SMs nearly empty and every candidate costs two
+// dependent loads (sorted id, then position). So a warp takes one particle:
+// each run of candidate slots goes 32 at a time, one candidate per lane, and
+// the lanes' terms are added in slot order (lowest lane first) with
+// shuffles. Every term is computed by the same float32 expression as the
+// sequential loop and added in the same order, so forward sums equal the
+// sequential ones bit for bit; reverse passes reduce their own-particle sums
+// with a shuffle tree (order free) and add partner terms with atomics.
+constexpr unsigned kFull = 0xffffffffu;
+
+inline unsigned warp_blocks(long long n) { return (unsigned)((n * 32 + kBlock - 1) / kBlock); }
+
+// The candidate runs of the (2R+1)^3 cells around `base` in the reference's
+// order: one run per (dz, dy) row, or one per cell (capped at kMaxCellScan)
+// when the row holds more than kMaxCellScan slots (as for_each_candidate).
+template <int R, class F>
+__device__ __forceinline__ void for_each_run(const SegParams &s, const uint32_t *__restrict__ off, int3 base, F &&f)
+{
+#pragma unroll 1
+  for (int dz = -R; dz <= R; ++dz) {
+    const int z = base.z + dz;
+    if (z < 0 || z >= s.nz) continue;
+#pragma unroll 1
+    for (int dy = -R; dy <= R; ++dy) {
+      const int y = base.y + dy;
+      if (y < 0 || y >= s.ny) continue;
+      const int x0 = max(base.x - R, 0), x1 = min(base.x + R, s.nx - 1);
+      const int row = s.c_begin + (z * s.ny + y) * s.nx;
+      const uint32_t a = __ldg(&off[row + x0]);
+      const uint32_t b = __ldg(&off[row + x1 + 1]);
+      if (b - a <= (uint32_t)kMaxCellScan) {
+        f(a, b);
+      } else {
+#pragma unroll 1
+        for (int x = x0; x <= x1; ++x) {
+          const uint32_t cs = __ldg(&off[row + x]);
+          uint32_t ce = __ldg(&off[row + x + 1]);
+          if (ce - cs > (uint32_t)kMaxCellScan) ce = cs + kMaxCellScan;
+          f(cs, ce);
+        }
+      }
+    }
+  }
+}
+
+// f(valid, j) on every lane of the warp for each chunk of 32 candidate slots,
+// lane l holding slot chunk + l (j = its particle id, -1 past the run).
+template <int R, class F>
+__device__ __forceinline__ void warp_chunks(const SegParams &s, const GridView &g, int3 base, int lane, F &&f)
+{
+  for_each_run<R>(s, g.off, base, [&](uint32_t a, uint32_t b) {
+#pragma unroll 1
+    for (uint32_t c = a; c < b; c += 32) {
+      const uint32_t k = c + (uint32_t)lane;
+      const bool valid = k < b;
+      f(valid, valid ? (int)__ldg(&g.ids[k]) : -1);
+    }
+  });
+}
+
+__device__ __forceinline__ float warp_sum(float v)
+{
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+
 // ---- forward passes (id order) ---------------------------------------------
 
 // sph_normal.glsl:24-81 over the previous substep's grid.
@@ -90,30 +159,47 @@ __global__ void __launch_bounds__(kBlock) k_ad_normal(const SegParams *__restric
                                                       const float *__restrict__ rho, int n,
                                                       float4 *__restrict__ out)
 {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (i >= n) return;
   const SegParams &s = segs[0];
   const float4 pi = pred[i];
   const float h = s.h, h2 = s.h2, mass = s.mass, poly6m6 = s.poly6m6, vlap = s.visclap;
   float nx = 0.0f, ny = 0.0f, nz = 0.0f, lap = 0.0f;
-  for_each_id<1>(s, g, cell_coord(s, pi.x, pi.y, pi.z), [&](int j) {
-    if (j == i) return;
-    const float4 pj = __ldg(&pred[j]);
-    const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-    const float r2 = dx * dx + dy * dy + dz * dz;
-    if (r2 >= h2) return;
-    const float rho_j = fmaxf(__ldg(&rho[j]), 1e-6f);
-    const float weight = mass / rho_j;
-    const float t = h2 - r2;
-    const float sg = poly6m6 * t * t;
-    nx += weight * (sg * dx);
-    ny += weight * (sg * dy);
-    nz += weight * (sg * dz);
-    lap += weight * w_visc_lap(sqrtf(r2), h, vlap);
+  warp_chunks<1>(s, g, cell_coord(s, pi.x, pi.y, pi.z), lane, [&](bool valid, int j) {
+    float tx = 0.0f, ty = 0.0f, tz = 0.0f, tl = 0.0f;
+    bool take = false;
+    if (valid && j != i) {
+      const float4 pj = __ldg(&pred[j]);
+      const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+      const float r2 = dx * dx + dy * dy + dz * dz;
+      if (r2 < h2) {
+        const float rho_j = fmaxf(__ldg(&rho[j]), 1e-6f);
+        const float weight = mass / rho_j;
+        const float t = h2 - r2;
+        const float sg = poly6m6 * t * t;
+        tx = weight * (sg * dx);
+        ty = weight * (sg * dy);
+        tz = weight * (sg * dz);
+        tl = weight * w_visc_lap(sqrtf(r2), h, vlap);
+        take = true;
+      }
+    }
+    unsigned m = __ballot_sync(kFull, take);
+    while (m) {
+      const int t = __ffs(m) - 1;
+      m &= m - 1;
+      nx += __shfl_sync(kFull, tx, t);
+      ny += __shfl_sync(kFull, ty, t);
+      nz += __shfl_sync(kFull, tz, t);
+      lap += __shfl_sync(kFull, tl, t);
+    }
   });
-  const float mag = sqrtf(nx * nx + ny * ny + nz * nz);
-  const float curv = (mag > 1e-4f) ? -lap / mag : 0.0f;
-  out[i] = make_float4(nx, ny, nz, curv);
+  if (lane == 0) {
+    const float mag = sqrtf(nx * nx + ny * ny + nz * nz);
+    const float curv = (mag > 1e-4f) ? -lap / mag : 0.0f;
+    out[i] = make_float4(nx, ny, nz, curv);
+  }
 }
 
 // sph_predict.glsl:23-57
@@ -137,31 +223,57 @@ __global__ void __launch_bounds__(kBlock) k_ad_lambda(const SegParams *__restric
                                                       const float4 *__restrict__ pred, int n,
                                                       float2 *__restrict__ lam, float4 *__restrict__ sq)
 {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (i >= n) return;
   const SegParams &s = segs[0];
   const float4 pi = pred[i];
   const float h = s.h, h2 = s.h2, mass = s.mass, poly6 = s.poly6, spiky = s.spiky;
   float density = 0.0f, gx = 0.0f, gy = 0.0f, gz = 0.0f, gn2 = 0.0f;
-  for_each_id<1>(s, g, cell_coord(s, pi.x, pi.y, pi.z), [&](int j) {
-    const float4 pj = __ldg(&pred[j]);
-    const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-    const float r2 = dx * dx + dy * dy + dz * dz;
-    density += mass * w_poly6(r2, h2, poly6);
-    if (j == i || r2 >= h2 || r2 <= 1e-12f) return;
-    const float r = sqrtf(r2);
-    const float sg = mass * w_spiky_grad(r, h, spiky);
-    const float ax = sg * (dx / r), ay = sg * (dy / r), az = sg * (dz / r);
-    gx += ax;
-    gy += ay;
-    gz += az;
-    gn2 += ax * ax + ay * ay + az * az;
+  warp_chunks<1>(s, g, cell_coord(s, pi.x, pi.y, pi.z), lane, [&](bool valid, int j) {
+    float td = 0.0f, ax = 0.0f, ay = 0.0f, az = 0.0f, an = 0.0f;
+    bool dens = false, grad = false;
+    if (valid) {
+      const float4 pj = __ldg(&pred[j]);
+      const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+      const float r2 = dx * dx + dy * dy + dz * dz;
+      if (r2 < h2) {  // out of range the sequential loop adds mass * 0
+        td = mass * w_poly6(r2, h2, poly6);
+        dens = true;
+      }
+      if (j != i && r2 < h2 && r2 > 1e-12f) {
+        const float r = sqrtf(r2);
+        const float sg = mass * w_spiky_grad(r, h, spiky);
+        ax = sg * (dx / r);
+        ay = sg * (dy / r);
+        az = sg * (dz / r);
+        an = ax * ax + ay * ay + az * az;
+        grad = true;
+      }
+    }
+    unsigned m = __ballot_sync(kFull, dens);
+    while (m) {
+      const int t = __ffs(m) - 1;
+      m &= m - 1;
+      density += __shfl_sync(kFull, td, t);
+    }
+    m = __ballot_sync(kFull, grad);
+    while (m) {
+      const int t = __ffs(m) - 1;
+      m &= m - 1;
+      gx += __shfl_sync(kFull, ax, t);
+      gy += __shfl_sync(kFull, ay, t);
+      gz += __shfl_sync(kFull, az, t);
+      gn2 += __shfl_sync(kFull, an, t);
+    }
   });
-  const float rest = s.rest;
-  const float constraint = fmaxf(density, 1e-6f) / rest - 1.0f;
-  const float denom = (gx * gx + gy * gy + gz * gz + gn2) / (rest * rest) + s.eps;
-  lam[i] = make_float2(fmaxf(density, 1e-6f), -constraint / fmaxf(denom, 1e-9f));
-  sq[i] = make_float4(gx, gy, gz, gn2);
+  if (lane == 0) {
+    const float rest = s.rest;
+    const float constraint = fmaxf(density, 1e-6f) / rest - 1.0f;
+    const float denom = (gx * gx + gy * gy + gz * gz + gn2) / (rest * rest) + s.eps;
+    lam[i] = make_float2(fmaxf(density, 1e-6f), -constraint / fmaxf(denom, 1e-9f));
+    sq[i] = make_float4(gx, gy, gz, gn2);
+  }
 }
 
 // sph_delta.glsl:19-85 + sph_apply_delta.glsl:10-20
@@ -170,7 +282,8 @@ __global__ void __launch_bounds__(kBlock) k_ad_delta_apply(const SegParams *__re
                                                            const float2 *__restrict__ lam, int n,
                                                            float4 *__restrict__ out)
 {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (i >= n) return;
   const SegParams &s = segs[0];
   const float4 pi = pred[i];
@@ -178,28 +291,43 @@ __global__ void __launch_bounds__(kBlock) k_ad_delta_apply(const SegParams *__re
   const float h = s.h, h2 = s.h2, spiky = s.spiky, poly6 = s.poly6, scorr_k = s.scorr_k, w_q = s.w_q;
   const bool use_scorr = scorr_k > 0.0f && w_q > 1e-9f;
   float ax = 0.0f, ay = 0.0f, az = 0.0f;
-  for_each_id<1>(s, g, cell_coord(s, pi.x, pi.y, pi.z), [&](int j) {
-    if (j == i) return;
-    const float4 pj = __ldg(&pred[j]);
-    const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-    const float r2 = dx * dx + dy * dy + dz * dz;
-    if (r2 >= h2 || r2 <= 1e-12f) return;
-    const float r = sqrtf(r2);
-    const float lambda_j = __ldg(&lam[j].y);
-    float s_corr = 0.0f;
-    if (use_scorr) {
-      const float ratio = w_poly6(r2, h2, poly6) / w_q;
-      const float rr = fmaxf(ratio, 0.0f);
-      const float rr2 = rr * rr;
-      s_corr = -scorr_k * (rr2 * rr2);
+  warp_chunks<1>(s, g, cell_coord(s, pi.x, pi.y, pi.z), lane, [&](bool valid, int j) {
+    float tx = 0.0f, ty = 0.0f, tz = 0.0f;
+    bool take = false;
+    if (valid && j != i) {
+      const float4 pj = __ldg(&pred[j]);
+      const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+      const float r2 = dx * dx + dy * dy + dz * dz;
+      if (r2 < h2 && r2 > 1e-12f) {
+        const float r = sqrtf(r2);
+        const float lambda_j = __ldg(&lam[j].y);
+        float s_corr = 0.0f;
+        if (use_scorr) {
+          const float ratio = w_poly6(r2, h2, poly6) / w_q;
+          const float rr = fmaxf(ratio, 0.0f);
+          const float rr2 = rr * rr;
+          s_corr = -scorr_k * (rr2 * rr2);
+        }
+        const float sc = (lambda_i + lambda_j + s_corr) * w_spiky_grad(r, h, spiky);
+        tx = sc * (dx / r);
+        ty = sc * (dy / r);
+        tz = sc * (dz / r);
+        take = true;
+      }
     }
-    const float sc = (lambda_i + lambda_j + s_corr) * w_spiky_grad(r, h, spiky);
-    ax += sc * (dx / r);
-    ay += sc * (dy / r);
-    az += sc * (dz / r);
+    unsigned m = __ballot_sync(kFull, take);
+    while (m) {
+      const int t = __ffs(m) - 1;
+      m &= m - 1;
+      ax += __shfl_sync(kFull, tx, t);
+      ay += __shfl_sync(kFull, ty, t);
+      az += __shfl_sync(kFull, tz, t);
+    }
   });
-  const float rest = s.rest;
-  out[i] = make_float4(pi.x + ax / rest, pi.y + ay / rest, pi.z + az / rest, 1.0f);
+  if (lane == 0) {
+    const float rest = s.rest;
+    out[i] = make_float4(pi.x + ax / rest, pi.y + ay / rest, pi.z + az / rest, 1.0f);
+  }
 }
 
 // sph_velocity.glsl + sph_xsph.glsl + sph_finalize.glsl. Keeps the velocity
@@ -214,7 +342,8 @@ __global__ void __launch_bounds__(kBlock) k_ad_final(const SegParams *__restrict
                                                      float4 *__restrict__ pos_next, float4 *__restrict__ vel_next,
                                                      float4 *__restrict__ pred_next, float *__restrict__ rho_next)
 {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (i >= n) return;
   const SegParams &s = segs[0];
   const float dtc = s.dtc, h2 = s.h2, mass = s.mass, poly6 = s.poly6;
@@ -222,21 +351,35 @@ __global__ void __launch_bounds__(kBlock) k_ad_final(const SegParams *__restrict
   const float4 p0 = pos[i];
   const float3 vi = make_float3((q.x - p0.x) / dtc, (q.y - p0.y) / dtc, (q.z - p0.z) / dtc);
   float ax = 0.0f, ay = 0.0f, az = 0.0f;
-  for_each_id<1>(s, g, cell_coord(s, q.x, q.y, q.z), [&](int j) {
-    if (j == i) return;
-    const float4 pj = __ldg(&pred[j]);
-    const float dx = q.x - pj.x, dy = q.y - pj.y, dz = q.z - pj.z;
-    const float r2 = dx * dx + dy * dy + dz * dz;
-    if (r2 >= h2) return;
-    const float rho_j = fmaxf(__ldg(&lam[j].x), 1e-6f);
-    const float4 xj = __ldg(&pos[j]);
-    const float vjx = (pj.x - xj.x) / dtc, vjy = (pj.y - xj.y) / dtc, vjz = (pj.z - xj.z) / dtc;
-    const float w = mass / rho_j;
-    const float wk = w_poly6(r2, h2, poly6);
-    ax += (w * (vjx - vi.x)) * wk;
-    ay += (w * (vjy - vi.y)) * wk;
-    az += (w * (vjz - vi.z)) * wk;
+  warp_chunks<1>(s, g, cell_coord(s, q.x, q.y, q.z), lane, [&](bool valid, int j) {
+    float tx = 0.0f, ty = 0.0f, tz = 0.0f;
+    bool take = false;
+    if (valid && j != i) {
+      const float4 pj = __ldg(&pred[j]);
+      const float dx = q.x - pj.x, dy = q.y - pj.y, dz = q.z - pj.z;
+      const float r2 = dx * dx + dy * dy + dz * dz;
+      if (r2 < h2) {
+        const float rho_j = fmaxf(__ldg(&lam[j].x), 1e-6f);
+        const float4 xj = __ldg(&pos[j]);
+        const float vjx = (pj.x - xj.x) / dtc, vjy = (pj.y - xj.y) / dtc, vjz = (pj.z - xj.z) / dtc;
+        const float w = mass / rho_j;
+        const float wk = w_poly6(r2, h2, poly6);
+        tx = (w * (vjx - vi.x)) * wk;
+        ty = (w * (vjy - vi.y)) * wk;
+        tz = (w * (vjz - vi.z)) * wk;
+        take = true;
+      }
+    }
+    unsigned m = __ballot_sync(kFull, take);
+    while (m) {
+      const int t = __ffs(m) - 1;
+      m &= m - 1;
+      ax += __shfl_sync(kFull, tx, t);
+      ay += __shfl_sync(kFull, ty, t);
+      az += __shfl_sync(kFull, tz, t);
+    }
   });
+  if (lane != 0) return;
   const float c = s.visc;
   float3 v = make_float3(vi.x + c * ax, vi.y + c * ay, vi.z + c * az);
   v_out[i] = make_float4(vi.x, vi.y, vi.z, 0.0f);
@@ -411,16 +554,17 @@ __global__ void __launch_bounds__(kBlock) k_rv_xsph(const SegParams *__restrict_
                                                     float4 *__restrict__ g_v, float4 *__restrict__ g_p,
                                                     float *__restrict__ g_rho)
 {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (i >= n) return;
   const SegParams &s = segs[0];
   const float h2 = s.h2, mass = s.mass, poly6 = s.poly6, c = s.visc;
   const float4 q = pred[i];
   const float3 vi = f3(v[i]);
   const float3 gvf = f3(g_vf[i]);
-  float3 acc_v = gvf, acc_p = make_float3(0.f, 0.f, 0.f);
-  for_each_id<1>(s, g, cell_coord(s, q.x, q.y, q.z), [&](int j) {
-    if (j == i) return;
+  float3 acc_v = make_float3(0.f, 0.f, 0.f), acc_p = make_float3(0.f, 0.f, 0.f);
+  warp_chunks<1>(s, g, cell_coord(s, q.x, q.y, q.z), lane, [&](bool valid, int j) {
+    if (!valid || j == i) return;
     const float4 pj = __ldg(&pred[j]);
     const float3 d = make_float3(q.x - pj.x, q.y - pj.y, q.z - pj.z);
     const float r2 = dot3(d, d);
@@ -439,8 +583,12 @@ __global__ void __launch_bounds__(kBlock) k_rv_xsph(const SegParams *__restrict_
     atomic_add3(&g_p[j], scale3(dd, -1.0f));
     atomicAdd(&g_rho[j], -c * (mass / (rho_j * rho_j)) * dot3(dv, gvf) * wk);
   });
-  atomic_add3(&g_v[i], acc_v);
-  atomic_add3(&g_p[i], acc_p);
+  acc_v = make_float3(warp_sum(acc_v.x), warp_sum(acc_v.y), warp_sum(acc_v.z));
+  acc_p = make_float3(warp_sum(acc_p.x), warp_sum(acc_p.y), warp_sum(acc_p.z));
+  if (lane == 0) {
+    atomic_add3(&g_v[i], add3(gvf, acc_v));
+    atomic_add3(&g_p[i], acc_p);
+  }
 }
 
 // Velocity reverse: v = (p - x) / dt.
@@ -468,7 +616,8 @@ __global__ void __launch_bounds__(kBlock) k_rv_delta(const SegParams *__restrict
                                                      const float4 *__restrict__ g_next, int n,
                                                      float4 *__restrict__ g_cur, float *__restrict__ g_lam)
 {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (i >= n) return;
   const SegParams &s = segs[0];
   const float h = s.h, h2 = s.h2, spiky = s.spiky, poly6 = s.poly6, scorr_k = s.scorr_k, w_q = s.w_q;
@@ -477,10 +626,10 @@ __global__ void __launch_bounds__(kBlock) k_rv_delta(const SegParams *__restrict
   const float lambda_i = lam[i].y;
   const float3 gn = f3(g_next[i]);
   const float3 a = scale3(gn, 1.0f / s.rest);
-  float3 acc_p = gn;
+  float3 acc_p = make_float3(0.f, 0.f, 0.f);
   float acc_l = 0.0f;
-  for_each_id<1>(s, g, cell_coord(s, pi.x, pi.y, pi.z), [&](int j) {
-    if (j == i) return;
+  warp_chunks<1>(s, g, cell_coord(s, pi.x, pi.y, pi.z), lane, [&](bool valid, int j) {
+    if (!valid || j == i) return;
     const float4 pj = __ldg(&pred[j]);
     const float3 d = make_float3(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z);
     const float r2 = dot3(d, d);
@@ -505,8 +654,12 @@ __global__ void __launch_bounds__(kBlock) k_rv_delta(const SegParams *__restrict
     acc_p = add3(acc_p, dd);
     atomic_add3(&g_cur[j], scale3(dd, -1.0f));
   });
-  atomic_add3(&g_cur[i], acc_p);
-  atomicAdd(&g_lam[i], acc_l);
+  acc_p = make_float3(warp_sum(acc_p.x), warp_sum(acc_p.y), warp_sum(acc_p.z));
+  acc_l = warp_sum(acc_l);
+  if (lane == 0) {
+    atomic_add3(&g_cur[i], add3(gn, acc_p));
+    atomicAdd(&g_lam[i], acc_l);
+  }
 }
 
 // Lambda reverse: lambda = -C / max(denom, 1e-9), C = max(rho, 1e-6) / rho0 - 1,
@@ -521,7 +674,8 @@ __global__ void __launch_bounds__(kBlock) k_rv_lambda(const SegParams *__restric
                                                       const float *__restrict__ g_rho_ext, int n,
                                                       float4 *__restrict__ g_cur)
 {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (i >= n) return;
   const SegParams &s = segs[0];
   const float h = s.h, h2 = s.h2, mass = s.mass, poly6 = s.poly6, spiky = s.spiky, rest = s.rest;
@@ -538,11 +692,11 @@ __global__ void __launch_bounds__(kBlock) k_rv_lambda(const SegParams *__restric
   if (!(li.x > 1e-6f)) grho = 0.0f;  // density clamped at 1e-6
   const float3 gS = scale3(S, 2.0f * gD / (rest * rest));
   const float gQ = gD / (rest * rest);
-  if (grho == 0.0f && gD == 0.0f) return;
+  if (grho == 0.0f && gD == 0.0f) return;  // uniform across the warp
   const float4 pi = pred[i];
   float3 acc = make_float3(0.f, 0.f, 0.f);
-  for_each_id<1>(s, g, cell_coord(s, pi.x, pi.y, pi.z), [&](int j) {
-    if (j == i) return;
+  warp_chunks<1>(s, g, cell_coord(s, pi.x, pi.y, pi.z), lane, [&](bool valid, int j) {
+    if (!valid || j == i) return;
     const float4 pj = __ldg(&pred[j]);
     const float3 d = make_float3(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z);
     const float r2 = dot3(d, d);
@@ -559,7 +713,8 @@ __global__ void __launch_bounds__(kBlock) k_rv_lambda(const SegParams *__restric
     acc = add3(acc, dd);
     atomic_add3(&g_cur[j], scale3(dd, -1.0f));
   });
-  atomic_add3(&g_cur[i], acc);
+  acc = make_float3(warp_sum(acc.x), warp_sum(acc.y), warp_sum(acc.z));
+  if (lane == 0) atomic_add3(&g_cur[i], acc);
 }
 
 // Predict reverse (sph_predict.glsl:23-57) with the normal pass's curvature
@@ -627,18 +782,19 @@ __global__ void __launch_bounds__(kBlock) k_rv_normal(const SegParams *__restric
                                                       const float4 *__restrict__ g_normal, int n,
                                                       float4 *__restrict__ g_pred, float *__restrict__ g_rho)
 {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (i >= n) return;
   const float4 gn4 = g_normal[i];
-  if (gn4.x == 0.0f && gn4.y == 0.0f && gn4.z == 0.0f && gn4.w == 0.0f) return;
+  if (gn4.x == 0.0f && gn4.y == 0.0f && gn4.z == 0.0f && gn4.w == 0.0f) return;  // uniform across the warp
   const SegParams &s = segs[0];
   const float h = s.h, h2 = s.h2, mass = s.mass, poly6m6 = s.poly6m6, vlap = s.visclap;
   const float3 gn = f3(gn4);
   const float glap = gn4.w;
   const float4 pi = pred[i];
   float3 acc = make_float3(0.f, 0.f, 0.f);
-  for_each_id<1>(s, g, cell_coord(s, pi.x, pi.y, pi.z), [&](int j) {
-    if (j == i) return;
+  warp_chunks<1>(s, g, cell_coord(s, pi.x, pi.y, pi.z), lane, [&](bool valid, int j) {
+    if (!valid || j == i) return;
     const float4 pj = __ldg(&pred[j]);
     const float3 d = make_float3(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z);
     const float r2 = dot3(d, d);
@@ -655,61 +811,65 @@ __global__ void __launch_bounds__(kBlock) k_rv_normal(const SegParams *__restric
     if (rj > 1e-6f)
       atomicAdd(&g_rho[j], -(mass / (rho_j * rho_j)) * (poly6m6 * t * t * dot3(d, gn) + vlap * (h - r) * glap));
   });
-  atomic_add3(&g_pred[i], acc);
+  acc = make_float3(warp_sum(acc.x), warp_sum(acc.y), warp_sum(acc.z));
+  if (lane == 0) atomic_add3(&g_pred[i], acc);
 }
 
-// Splat reverse, gathered per particle over the samples its kernel reaches:
-// value(x) = sum_j m W(|x - p_j|^2) / rho0 over the candidates of x's cells.
+// Splat reverse, gathered per particle (one warp, lanes over the samples its
+// kernel reaches): value(x) = sum_j m W(|x - p_j|^2) / rho0 over the
+// candidates of x's cells.
 __global__ void __launch_bounds__(kBlock) k_rv_splat(const SegParams *__restrict__ segs, GridView g, SplatGeom sp,
                                                      const float4 *__restrict__ pos,
                                                      const uint8_t *__restrict__ collider,
                                                      const float *__restrict__ g_surface, int n,
                                                      float4 *__restrict__ g_pos)
 {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (j >= n) return;
   const SegParams &s = segs[0];
   const float4 pj = pos[j];
   const uint32_t cj = g.cell[j];
   const int cjx = (int)(cj % (uint32_t)s.nx), cjy = (int)((cj / (uint32_t)s.nx) % (uint32_t)s.ny),
             cjz = (int)(cj / ((uint32_t)s.nx * (uint32_t)s.ny));
-  const uint32_t slot = g.slot[j];
-  const bool capped = slot >= __ldg(&g.off[cj]) + (uint32_t)kMaxCellScan;
-  if (capped) return;  // beyond the per-cell scan limit: never a candidate
+  if (g.slot[j] >= __ldg(&g.off[cj]) + (uint32_t)kMaxCellScan) return;  // beyond the per-cell scan limit
   const float scale = sp.mass / fmaxf(sp.rest, 1e-6f) * 6.0f * sp.kcoef;
-  int lo[3], hi[3];
+  int lo[3], ext[3];
   const float pc[3] = {pj.x, pj.y, pj.z}, sl[3] = {sp.slox, sp.sloy, sp.sloz};
   const int dims[3] = {sp.snx, sp.sny, sp.snz};
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     lo[a] = max((int)floorf((pc[a] - sp.kr - sl[a]) / sp.spacing) - 1, 0);
-    hi[a] = min((int)floorf((pc[a] + sp.kr - sl[a]) / sp.spacing) + 1, dims[a] - 1);
+    ext[a] = max(min((int)floorf((pc[a] + sp.kr - sl[a]) / sp.spacing) + 1, dims[a] - 1) - lo[a] + 1, 0);
   }
+  const int total = ext[0] * ext[1] * ext[2];
   float3 acc = make_float3(0.f, 0.f, 0.f);
-  for (int gz = lo[2]; gz <= hi[2]; ++gz)
-    for (int gy = lo[1]; gy <= hi[1]; ++gy)
-      for (int gx = lo[0]; gx <= hi[0]; ++gx) {
-        const float px = sp.slox + (float)gx * sp.spacing;
-        const float py = sp.sloy + (float)gy * sp.spacing;
-        const float pz = sp.sloz + (float)gz * sp.spacing;
-        const float dx = px - pj.x, dy = py - pj.y, dz = pz - pj.z;
-        const float r2 = dx * dx + dy * dy + dz * dz;
-        if (r2 >= sp.kh2) continue;
-        const int3 b = cell_coord(s, px, py, pz);
-        if (abs(b.x - cjx) > kSurfaceCellRadius || abs(b.y - cjy) > kSurfaceCellRadius ||
-            abs(b.z - cjz) > kSurfaceCellRadius)
-          continue;
-        if (s.voxel > 0.0f) {
-          const int3 c = collider_coord(s, px, py, pz);
-          if (collider_occupied(s, collider, c.x, c.y, c.z)) continue;
-        }
-        const long long t = ((long long)gz * sp.sny + gy) * sp.snx + gx;
-        const float tt = sp.kh2 - r2;
-        const float k = g_surface[t] * scale * tt * tt;
-        acc = add3(acc, make_float3(k * dx, k * dy, k * dz));
-      }
-  float4 gp = g_pos[j];
-  g_pos[j] = make_float4(gp.x + acc.x, gp.y + acc.y, gp.z + acc.z, 0.0f);
+  for (int u = lane; u < total; u += 32) {
+    const int gx = lo[0] + u % ext[0], gy = lo[1] + (u / ext[0]) % ext[1], gz = lo[2] + u / (ext[0] * ext[1]);
+    const float px = sp.slox + (float)gx * sp.spacing;
+    const float py = sp.sloy + (float)gy * sp.spacing;
+    const float pz = sp.sloz + (float)gz * sp.spacing;
+    const float dx = px - pj.x, dy = py - pj.y, dz = pz - pj.z;
+    const float r2 = dx * dx + dy * dy + dz * dz;
+    if (r2 >= sp.kh2) continue;
+    const int3 b = cell_coord(s, px, py, pz);
+    if (abs(b.x - cjx) > kSurfaceCellRadius || abs(b.y - cjy) > kSurfaceCellRadius ||
+        abs(b.z - cjz) > kSurfaceCellRadius)
+      continue;
+    if (s.voxel > 0.0f) {
+      const int3 c = collider_coord(s, px, py, pz);
+      if (collider_occupied(s, collider, c.x, c.y, c.z)) continue;
+    }
+    const long long t = ((long long)gz * sp.sny + gy) * sp.snx + gx;
+    const float tt = sp.kh2 - r2;
+    const float k = g_surface[t] * scale * tt * tt;
+    acc = add3(acc, make_float3(k * dx, k * dy, k * dz));
+  }
+  acc = make_float3(warp_sum(acc.x), warp_sum(acc.y), warp_sum(acc.z));
+  if (lane == 0) {
+    const float4 gp = g_pos[j];
+    g_pos[j] = make_float4(gp.x + acc.x, gp.y + acc.y, gp.z + acc.z, 0.0f);
+  }
 }
 
 __global__ void k_combine_initial(const float4 *__restrict__ g_pos, const float4 *__restrict__ g_pred,
@@ -911,9 +1071,9 @@ struct Adjoint {
   // finalized state into checkpoint s + 1. build = build grid s + 1 (forward).
   void substep(int s, bool build)
   {
-    const unsigned nb = blocks_for(n);
+    const unsigned nb = blocks_for(n), nw = warp_blocks(n);
     if (seg.sigma > 0.0f) {
-      k_ad_normal<<<nb, kBlock, 0, stream>>>(d_seg, grid(s), ckp(ck_pred, s), ckr(s), n, w_normal);
+      k_ad_normal<<<nw, kBlock, 0, stream>>>(d_seg, grid(s), ckp(ck_pred, s), ckr(s), n, w_normal);
       g_launches += 1;
     }
     k_ad_predict<<<nb, kBlock, 0, stream>>>(d_seg, ckp(ck_pos, s), ckp(ck_vel, s), w_normal, n, wp(0));
@@ -921,10 +1081,10 @@ struct Adjoint {
     if (build) build_grid(s + 1, wp(0));
     const GridView g = grid(s + 1);
     for (int t = 0; t < iterations; ++t) {
-      k_ad_lambda<<<nb, kBlock, 0, stream>>>(d_seg, g, wp(t), n, wl(t), wsq(t));
-      k_ad_delta_apply<<<nb, kBlock, 0, stream>>>(d_seg, g, wp(t), wl(t), n, wp(t + 1));
+      k_ad_lambda<<<nw, kBlock, 0, stream>>>(d_seg, g, wp(t), n, wl(t), wsq(t));
+      k_ad_delta_apply<<<nw, kBlock, 0, stream>>>(d_seg, g, wp(t), wl(t), n, wp(t + 1));
     }
-    k_ad_final<<<nb, kBlock, 0, stream>>>(d_seg, g, wp(iterations), ckp(ck_pos, s), wl(iterations - 1), collider, n,
+    k_ad_final<<<nw, kBlock, 0, stream>>>(d_seg, g, wp(iterations), ckp(ck_pos, s), wl(iterations - 1), collider, n,
                                           w_v, w_vf, ckp(ck_pos, s + 1), ckp(ck_vel, s + 1),
                                           ckp(ck_pred, s + 1), ckr(s + 1));
     g_launches += 2 * iterations + 2;
@@ -935,7 +1095,7 @@ struct Adjoint {
   // (g_*_in).
   void reverse(int s)
   {
-    const unsigned nb = blocks_for(n);
+    const unsigned nb = blocks_for(n), nw = warp_blocks(n);
     const size_t f4 = N() * sizeof(float4), f1 = N() * sizeof(float);
     const GridView g = grid(s + 1);
     cudaMemsetAsync(g_v, 0, f4, stream);
@@ -944,15 +1104,15 @@ struct Adjoint {
     cudaMemcpyAsync(g_rho_t, g_rho_out, f1, cudaMemcpyDeviceToDevice, stream);
     k_rv_final<<<nb, kBlock, 0, stream>>>(d_seg, wp(iterations), w_vf, collider, g_pos_out, g_vel_out, g_pred_out, n,
                                           g_pa, g_vf);
-    k_rv_xsph<<<nb, kBlock, 0, stream>>>(d_seg, g, wp(iterations), w_v, wl(iterations - 1), g_vf, n, g_v, g_pa,
+    k_rv_xsph<<<nw, kBlock, 0, stream>>>(d_seg, g, wp(iterations), w_v, wl(iterations - 1), g_vf, n, g_v, g_pa,
                                          g_rho_t);
     k_rv_velocity<<<nb, kBlock, 0, stream>>>(d_seg, g_v, n, g_pa, g_pos_in);
     g_launches += 3;
     for (int t = iterations - 1; t >= 0; --t) {
       cudaMemsetAsync(g_pb, 0, f4, stream);
       cudaMemsetAsync(g_lam, 0, f1, stream);
-      k_rv_delta<<<nb, kBlock, 0, stream>>>(d_seg, g, wp(t), wl(t), g_pa, n, g_pb, g_lam);
-      k_rv_lambda<<<nb, kBlock, 0, stream>>>(d_seg, g, wp(t), wl(t), wsq(t), g_lam,
+      k_rv_delta<<<nw, kBlock, 0, stream>>>(d_seg, g, wp(t), wl(t), g_pa, n, g_pb, g_lam);
+      k_rv_lambda<<<nw, kBlock, 0, stream>>>(d_seg, g, wp(t), wl(t), wsq(t), g_lam,
                                              t == iterations - 1 ? g_rho_t : nullptr, n, g_pb);
       g_launches += 2;
       std::swap(g_pa, g_pb);
@@ -960,7 +1120,7 @@ struct Adjoint {
     k_rv_predict<<<nb, kBlock, 0, stream>>>(d_seg, ckp(ck_vel, s), w_normal, g_pa, n, g_pos_in, g_vel_in, g_normal);
     g_launches += 1;
     if (seg.sigma > 0.0f) {
-      k_rv_normal<<<nb, kBlock, 0, stream>>>(d_seg, grid(s), ckp(ck_pred, s), ckr(s), g_normal, n, g_pred_in,
+      k_rv_normal<<<nw, kBlock, 0, stream>>>(d_seg, grid(s), ckp(ck_pred, s), ckr(s), g_normal, n, g_pred_in,
                                              g_rho_in);
       g_launches += 1;
     }
@@ -1202,7 +1362,7 @@ int flowx_substep_adjoint(flowx_adjoint *adj, const float *surface_grad, const f
       cudaMemsetAsync(a->g_pred_out, 0, f4, st);
       cudaMemsetAsync(a->g_rho_out, 0, f1, st);
       if (a->splat_on) {
-        k_rv_splat<<<blocks_for(a->n), kBlock, 0, st>>>(a->d_seg, a->grid(S), a->sp, a->ckp(a->ck_pos, S),
+        k_rv_splat<<<warp_blocks(a->n), kBlock, 0, st>>>(a->d_seg, a->grid(S), a->sp, a->ckp(a->ck_pos, S),
                                                         a->collider, a->g_surface, a->n, a->g_pos_out);
         g_launches += 1;
       }
