@@ -14,9 +14,18 @@
 //   phase 2 - run the pass body over the set bits, rows in order, slots
 //             ascending.
 // Phase 2 visits exactly the candidates the body would accept, in the
-// reference's (row, slot) order, so the result equals a single scan's. A row
-// longer than 64 slots (dense regions, or a cell above the reference's
-// MAX_CELL_SCAN) is walked directly instead.
+// reference's (row, slot) order, so the result equals a single scan's.
+//
+// Phase 1 runs over all nine rows first and leaves their masks in shared
+// memory (nine 64-bit words per thread); phase 2 is then one loop over every
+// set bit of every row, each lane moving to its next row when its current
+// mask runs out. A warp so runs the body (busiest lane's accepted total)
+// times instead of the sum over rows of the busiest lane's per-row count,
+// which at 8-10 particles per cell is about 45 instead of 75.
+//
+// A particle with a row longer than 64 slots (dense regions, or a cell above
+// the reference's MAX_CELL_SCAN) takes the per-row walk, which handles such
+// rows by walking them directly.
 #pragma once
 
 #include "pbf_math.cuh"
@@ -38,9 +47,9 @@ __device__ __forceinline__ float pair_r2(float dx, float dy, float dz)
 // walked directly with the reference's per-cell MAX_CELL_SCAN cap, calling
 // f for every candidate of the row (the body repeats its own test).
 template <bool EXACT, class F>
-__device__ __forceinline__ void for_each_within(const SegParams &s, const uint32_t *__restrict__ off,
-                                                const float4 *__restrict__ pos, float4 p, float lim2, int3 base,
-                                                F &&f)
+__device__ __forceinline__ void for_each_within_rows(const SegParams &s, const uint32_t *__restrict__ off,
+                                                     const float4 *__restrict__ pos, float4 p, float lim2,
+                                                     int3 base, F &&f)
 {
   const int x0 = max(base.x - 1, 0), x1 = min(base.x + 1, s.nx - 1);
 #pragma unroll 1
@@ -77,6 +86,69 @@ __device__ __forceinline__ void for_each_within(const SegParams &s, const uint32
       mm &= mm - 1ull;
       f((int)ra + t);
     }
+  }
+}
+
+// Dynamic shared memory a neighbour-pass launch of `block` threads needs:
+// the row masks, nine per thread, laid out row-major across the block.
+inline size_t row_mask_bytes(int block) { return (size_t)block * kRows * sizeof(unsigned long long); }
+
+// The two-phase walk with phase 2 flattened across rows (see the top of this
+// file); launches must provide row_mask_bytes(blockDim.x) of dynamic shared
+// memory. Same visits, same order as for_each_within_rows.
+template <bool EXACT, class F>
+__device__ __forceinline__ void for_each_within(const SegParams &s, const uint32_t *__restrict__ off,
+                                                const float4 *__restrict__ pos, float4 p, float lim2, int3 base,
+                                                F &&f)
+{
+  extern __shared__ unsigned long long row_masks[];
+  unsigned long long *mine = row_masks + threadIdx.x;
+  const int stride = blockDim.x;
+  const int x0 = max(base.x - 1, 0), x1 = min(base.x + 1, s.nx - 1);
+  bool wide = false;
+#pragma unroll 1
+  for (int r = 0; r < kRows; ++r) {
+    const int z = base.z + (r / 3) - 1;
+    const int y = base.y + (r % 3) - 1;
+    unsigned long long mm = 0ull;
+    if (z >= 0 && z < s.nz && y >= 0 && y < s.ny) {
+      const int row = s.c_begin + (z * s.ny + y) * s.nx;
+      const uint32_t ra = __ldg(&off[row + x0]);
+      const uint32_t rb = __ldg(&off[row + x1 + 1]);
+      if (rb - ra > 64u) {
+        wide = true;
+        break;
+      }
+#pragma unroll 4
+      for (uint32_t k = ra; k < rb; ++k) {
+        const float4 q = __ldg(&pos[k]);
+        const float r2 = pair_r2<EXACT>(p.x - q.x, p.y - q.y, p.z - q.z);
+        if (r2 < lim2) mm |= 1ull << (k - ra);
+      }
+    }
+    mine[r * stride] = mm;
+  }
+  if (wide) {
+    for_each_within_rows<EXACT>(s, off, pos, p, lim2, base, f);
+    return;
+  }
+  int r = -1;
+  unsigned long long m = 0ull;
+  uint32_t ra = 0;
+#pragma unroll 1
+  while (true) {
+    if (m == 0ull) {
+      do {
+        ++r;
+      } while (r < kRows && (m = mine[r * stride]) == 0ull);
+      if (r >= kRows) break;
+      const int z = base.z + (r / 3) - 1;
+      const int y = base.y + (r % 3) - 1;
+      ra = __ldg(&off[s.c_begin + (z * s.ny + y) * s.nx + x0]);
+    }
+    const int t = __ffsll((long long)m) - 1;
+    m &= m - 1ull;
+    f((int)ra + t);
   }
 }
 

@@ -196,16 +196,16 @@ void launch_lambda_f(const DeviceState &d, const float4 *pred, bool exact, cudaS
 {
   const int b = FLOWX_BLOCK(d, K_LAMBDA, 128, exact ? (const void *)k_lambda_f<true> : (const void *)k_lambda_f<false>);
   if (d.n <= 0) return;
-  if (exact) k_lambda_f<true><<<grid_for(d.n, b), b, 0, st>>>(d, pred);
-  else k_lambda_f<false><<<grid_for(d.n, b), b, 0, st>>>(d, pred);
+  if (exact) k_lambda_f<true><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred);
+  else k_lambda_f<false><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred);
 }
 void launch_delta_apply_f(const DeviceState &d, const float4 *pred_in, float4 *pred_out, bool exact, cudaStream_t st)
 {
   const int b = FLOWX_BLOCK(d, K_DELTA_APPLY, 128,
                             exact ? (const void *)k_delta_apply_f<true> : (const void *)k_delta_apply_f<false>);
   if (d.n <= 0) return;
-  if (exact) k_delta_apply_f<true><<<grid_for(d.n, b), b, 0, st>>>(d, pred_in, pred_out);
-  else k_delta_apply_f<false><<<grid_for(d.n, b), b, 0, st>>>(d, pred_in, pred_out);
+  if (exact) k_delta_apply_f<true><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred_in, pred_out);
+  else k_delta_apply_f<false><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred_in, pred_out);
 }
 void launch_xsph_finalize_f(const DeviceState &d, const float4 *pred, const float4 *pos_in, float4 *pos_out,
                             bool keep_delta, bool exact, cudaStream_t st)
@@ -213,15 +213,15 @@ void launch_xsph_finalize_f(const DeviceState &d, const float4 *pred, const floa
   const int b = FLOWX_BLOCK(d, K_XSPH_FINALIZE, 128,
                             exact ? (const void *)k_xsph_finalize_f<true> : (const void *)k_xsph_finalize_f<false>);
   if (d.n <= 0) return;
-  if (exact) k_xsph_finalize_f<true><<<grid_for(d.n, b), b, 0, st>>>(d, pred, pos_in, pos_out, keep_delta);
-  else k_xsph_finalize_f<false><<<grid_for(d.n, b), b, 0, st>>>(d, pred, pos_in, pos_out, keep_delta);
+  if (exact) k_xsph_finalize_f<true><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred, pos_in, pos_out, keep_delta);
+  else k_xsph_finalize_f<false><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred, pos_in, pos_out, keep_delta);
 }
 void launch_normal_f(const DeviceState &d, const float4 *pred, float4 *out, bool exact, cudaStream_t st)
 {
   const int b = FLOWX_BLOCK(d, K_NORMAL, 128, exact ? (const void *)k_normal_f<true> : (const void *)k_normal_f<false>);
   if (d.n <= 0) return;
-  if (exact) k_normal_f<true><<<grid_for(d.n, b), b, 0, st>>>(d, pred, out);
-  else k_normal_f<false><<<grid_for(d.n, b), b, 0, st>>>(d, pred, out);
+  if (exact) k_normal_f<true><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred, out);
+  else k_normal_f<false><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred, out);
 }
 
 // ---- single reference passes (per-pass API; always exact) ------------------
@@ -295,7 +295,7 @@ void launch_predict(const DeviceState &d, float4 *pred, cudaStream_t st)
 void launch_delta(const DeviceState &d, const float4 *pred, cudaStream_t st)
 {
   const int b = FLOWX_BLOCK(d, K_DELTA, 128, k_delta);
-  if (d.n > 0) k_delta<<<grid_for(d.n, b), b, 0, st>>>(d, pred);
+  if (d.n > 0) k_delta<<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred);
 }
 void launch_apply(const DeviceState &d, float4 *pred, cudaStream_t st)
 {
@@ -308,7 +308,7 @@ void launch_velocity(const DeviceState &d, const float4 *pred, cudaStream_t st)
 void launch_xsph(const DeviceState &d, const float4 *pred, cudaStream_t st)
 {
   const int b = FLOWX_BLOCK(d, K_XSPH, 128, k_xsph);
-  if (d.n > 0) k_xsph<<<grid_for(d.n, b), b, 0, st>>>(d, pred);
+  if (d.n > 0) k_xsph<<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred);
 }
 void launch_finalize(const DeviceState &d, const float4 *pred, cudaStream_t st)
 {
