@@ -49,6 +49,8 @@ struct SegParams {
   float dtc;                   // max(dt, 1e-6)
   float scorr_k, sigma;        // i_sort.z / .w as floats
   float poly6, poly6m6, spiky, visclap, w_q, v_max;
+  // products the re-associated (FAST) pair bodies use, formed once on the host
+  float mass_spiky, mass_poly6, poly6_over_wq;
   int col_nx, col_ny, col_nz;  // i_collider.xyz
   float voxel;                 // i_collider.w as float; 0 = no collider
   long long col_begin;         // byte offset of this segment's voxels

@@ -119,12 +119,29 @@ __device__ __forceinline__ void for_each_within(const SegParams &s, const uint32
         wide = true;
         break;
       }
-#pragma unroll 4
-      for (uint32_t k = ra; k < rb; ++k) {
-        const float4 q = __ldg(&pos[k]);
-        const float r2 = pair_r2<EXACT>(p.x - q.x, p.y - q.y, p.z - q.z);
-        if (r2 < lim2) mm |= 1ull << (k - ra);
+      // four candidates per step: their accept bits packed into a nibble
+      // and or-ed into the 32-bit half of the mask it falls in (offsets
+      // are multiples of four, so a nibble never straddles the halves)
+      uint32_t lo = 0u, hi = 0u;
+      const uint32_t len = rb - ra;
+#pragma unroll 1
+      for (uint32_t o = 0; o < len; o += 4) {
+        uint32_t nib = 0u;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const uint32_t k = ra + o + (uint32_t)u;
+          if (o + (uint32_t)u < len) {
+            const float4 q = __ldg(&pos[k]);
+            const float r2 = pair_r2<EXACT>(p.x - q.x, p.y - q.y, p.z - q.z);
+            nib |= (r2 < lim2 ? 1u : 0u) << u;
+          }
+        }
+        if (o < 32u)
+          lo |= nib << o;
+        else
+          hi |= nib << (o - 32u);
       }
+      mm = ((unsigned long long)hi << 32) | lo;
     }
     mine[r * stride] = mm;
   }
@@ -186,7 +203,7 @@ struct LambdaAcc {
       if (self || r2 <= 1e-12f) return;
       const float rinv = rsqrtf(r2);
       const float hr = __fsub_rn(s.h, __fmul_rn(r2, rinv));
-      const float g = __fmul_rn(__fmul_rn(s.mass * s.spiky, __fmul_rn(hr, hr)), rinv);
+      const float g = __fmul_rn(__fmul_rn(s.mass_spiky, __fmul_rn(hr, hr)), rinv);
       gx = __fmaf_rn(g, dx, gx);
       gy = __fmaf_rn(g, dy, gy);
       gz = __fmaf_rn(g, dz, gz);
@@ -227,7 +244,7 @@ __device__ __forceinline__ void delta_pair(const SegParams &s, float lambda_i, f
     float lam = __fadd_rn(lambda_i, lambda_j);
     if (s.scorr_k > 0.0f && s.w_q > 1e-9f) {
       const float t = __fsub_rn(s.h2, r2);
-      const float ratio = __fmul_rn(__fmul_rn(__fmul_rn(t, t), t), s.poly6 / s.w_q);
+      const float ratio = __fmul_rn(__fmul_rn(__fmul_rn(t, t), t), s.poly6_over_wq);
       const float rr2 = __fmul_rn(ratio, ratio);
       lam = __fmaf_rn(-s.scorr_k, __fmul_rn(rr2, rr2), lam);
     }

@@ -107,7 +107,7 @@ __device__ __forceinline__ float3 xsph_sum_f(const SegParams &s, const DeviceSta
       az += (w * (vj.z - vi.z)) * wk;
     } else {
       const float t = __fsub_rn(h2, r2);
-      const float wk = __fmul_rn(__fdividef(mass * poly6, rho_j), __fmul_rn(__fmul_rn(t, t), t));
+      const float wk = __fmul_rn(__fdividef(s.mass_poly6, rho_j), __fmul_rn(__fmul_rn(t, t), t));
       ax = __fmaf_rn(wk, __fsub_rn(vj.x, vi.x), ax);
       ay = __fmaf_rn(wk, __fsub_rn(vj.y, vi.y), ay);
       az = __fmaf_rn(wk, __fsub_rn(vj.z, vi.z), az);

@@ -103,6 +103,9 @@ void seg_from_push(const flowx_push &p, SegParams &s)
     }
   }
   s.v_max = 0.4f * s.h / std::fmax(s.dt, 1e-6f);
+  s.mass_spiky = s.mass * s.spiky;
+  s.mass_poly6 = s.mass * s.poly6;
+  s.poly6_over_wq = s.w_q > 1e-9f ? s.poly6 / s.w_q : 0.0f;
   s.col_nx = p.i_collider[0];
   s.col_ny = p.i_collider[1];
   s.col_nz = p.i_collider[2];
