@@ -121,6 +121,8 @@ struct DeviceState {
   uint32_t *big_cells;      // [0] = count, then cell indices
   uint8_t *collider;
   float *surface;
+  unsigned long long *row_masks;  // the lambda pass's neighbour masks, 9 per slot (row-major)
+  uint8_t *row_wide;        // per slot: masks not recorded (a row over 64 slots)
   const SegParams *segs;
   int nseg;
   int n;                    // total particles

@@ -93,19 +93,15 @@ __device__ __forceinline__ void for_each_within_rows(const SegParams &s, const u
 // the row masks, nine per thread, laid out row-major across the block.
 inline size_t row_mask_bytes(int block) { return (size_t)block * kRows * sizeof(unsigned long long); }
 
-// The two-phase walk with phase 2 flattened across rows (see the top of this
-// file); launches must provide row_mask_bytes(blockDim.x) of dynamic shared
-// memory. Same visits, same order as for_each_within_rows.
-template <bool EXACT, class F>
-__device__ __forceinline__ void for_each_within(const SegParams &s, const uint32_t *__restrict__ off,
+// Phase 1 of all nine rows into this thread's shared masks (mine[r * stride]).
+// Returns false, leaving the masks incomplete, when a row is wider than 64
+// slots (the particle then takes the per-row walk).
+template <bool EXACT>
+__device__ __forceinline__ bool build_row_masks(const SegParams &s, const uint32_t *__restrict__ off,
                                                 const float4 *__restrict__ pos, float4 p, float lim2, int3 base,
-                                                F &&f)
+                                                unsigned long long *mine, int stride)
 {
-  extern __shared__ unsigned long long row_masks[];
-  unsigned long long *mine = row_masks + threadIdx.x;
-  const int stride = blockDim.x;
   const int x0 = max(base.x - 1, 0), x1 = min(base.x + 1, s.nx - 1);
-  bool wide = false;
 #pragma unroll 1
   for (int r = 0; r < kRows; ++r) {
     const int z = base.z + (r / 3) - 1;
@@ -115,10 +111,7 @@ __device__ __forceinline__ void for_each_within(const SegParams &s, const uint32
       const int row = s.c_begin + (z * s.ny + y) * s.nx;
       const uint32_t ra = __ldg(&off[row + x0]);
       const uint32_t rb = __ldg(&off[row + x1 + 1]);
-      if (rb - ra > 64u) {
-        wide = true;
-        break;
-      }
+      if (rb - ra > 64u) return false;
       // four candidates per step: their accept bits packed into a nibble
       // and or-ed into the 32-bit half of the mask it falls in (offsets
       // are multiples of four, so a nibble never straddles the halves)
@@ -145,10 +138,16 @@ __device__ __forceinline__ void for_each_within(const SegParams &s, const uint32
     }
     mine[r * stride] = mm;
   }
-  if (wide) {
-    for_each_within_rows<EXACT>(s, off, pos, p, lim2, base, f);
-    return;
-  }
+  return true;
+}
+
+// Phase 2: every set bit of every row, rows in order, slots ascending; each
+// lane moves to its next row when its current mask runs out.
+template <class F>
+__device__ __forceinline__ void visit_row_masks(const SegParams &s, const uint32_t *__restrict__ off, int3 base,
+                                                const unsigned long long *mine, int stride, F &&f)
+{
+  const int x0 = max(base.x - 1, 0);
   int r = -1;
   unsigned long long m = 0ull;
   uint32_t ra = 0;
@@ -167,6 +166,71 @@ __device__ __forceinline__ void for_each_within(const SegParams &s, const uint32
     m &= m - 1ull;
     f((int)ra + t);
   }
+}
+
+// The two-phase walk with phase 2 flattened across rows (see the top of this
+// file); launches must provide row_mask_bytes(blockDim.x) of dynamic shared
+// memory. Same visits, same order as for_each_within_rows.
+template <bool EXACT, class F>
+__device__ __forceinline__ void for_each_within(const SegParams &s, const uint32_t *__restrict__ off,
+                                                const float4 *__restrict__ pos, float4 p, float lim2, int3 base,
+                                                F &&f)
+{
+  extern __shared__ unsigned long long row_masks[];
+  unsigned long long *mine = row_masks + threadIdx.x;
+  if (build_row_masks<EXACT>(s, off, pos, p, lim2, base, mine, blockDim.x))
+    visit_row_masks(s, off, base, mine, blockDim.x, f);
+  else
+    for_each_within_rows<EXACT>(s, off, pos, p, lim2, base, f);
+}
+
+// Row masks one pass leaves for a later pass that tests the same positions
+// against the same grid with the same reach (the lambda and delta passes of
+// one Jacobi iteration): nine masks per slot, masks[r * n + slot], and a flag
+// for particles that took the per-row walk.
+struct MaskRecord {
+  unsigned long long *masks;
+  uint8_t *wide;
+  int n;
+};
+
+// for_each_within that also records slot i's masks.
+template <bool EXACT, class F>
+__device__ __forceinline__ void for_each_within_recording(const SegParams &s, const uint32_t *__restrict__ off,
+                                                          const float4 *__restrict__ pos, float4 p, float lim2,
+                                                          int3 base, MaskRecord rec, int i, F &&f)
+{
+  extern __shared__ unsigned long long row_masks[];
+  unsigned long long *mine = row_masks + threadIdx.x;
+  const int stride = blockDim.x;
+  const bool ok = build_row_masks<EXACT>(s, off, pos, p, lim2, base, mine, stride);
+  rec.wide[i] = ok ? 0 : 1;
+  if (ok) {
+#pragma unroll
+    for (int r = 0; r < kRows; ++r) rec.masks[(size_t)r * rec.n + i] = mine[r * stride];
+    visit_row_masks(s, off, base, mine, stride, f);
+  } else {
+    for_each_within_rows<EXACT>(s, off, pos, p, lim2, base, f);
+  }
+}
+
+// for_each_within from slot i's recorded masks (same positions, grid and
+// reach as the recording pass): phase 2 only.
+template <bool EXACT, class F>
+__device__ __forceinline__ void for_each_within_recorded(const SegParams &s, const uint32_t *__restrict__ off,
+                                                         const float4 *__restrict__ pos, float4 p, float lim2,
+                                                         int3 base, MaskRecord rec, int i, F &&f)
+{
+  extern __shared__ unsigned long long row_masks[];
+  unsigned long long *mine = row_masks + threadIdx.x;
+  const int stride = blockDim.x;
+  if (__ldg(&rec.wide[i])) {
+    for_each_within_rows<EXACT>(s, off, pos, p, lim2, base, f);
+    return;
+  }
+#pragma unroll
+  for (int r = 0; r < kRows; ++r) mine[r * stride] = __ldg(&rec.masks[(size_t)r * rec.n + i]);
+  visit_row_masks(s, off, base, mine, stride, f);
 }
 
 // ---- pass bodies ----------------------------------------------------------

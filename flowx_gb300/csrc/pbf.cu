@@ -43,15 +43,19 @@ __global__ void __launch_bounds__(512) k_lambda_f(DeviceState d, const float4 *_
   const float4 pi = pred[i];
   const int3 base = cell_coord(s, pi.x, pi.y, pi.z);
   LambdaAcc<EXACT> acc;
-  for_each_within<EXACT>(s, d.offsets, pred, pi, s.h2, base, [&](int k) {
+  const MaskRecord rec{d.row_masks, d.row_wide, d.n};
+  for_each_within_recording<EXACT>(s, d.offsets, pred, pi, s.h2, base, rec, i, [&](int k) {
     const float4 pj = __ldg(&pred[k]);
     acc.pair(s, pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, k == i);
   });
   d.lam[i] = acc.finish(s);
 }
 
-// sph_delta.glsl:19-85, summed correction before the 1/rho0 scale.
-template <bool EXACT>
+// sph_delta.glsl:19-85, summed correction before the 1/rho0 scale. RECORDED:
+// the lambda pass of this iteration just tested the same positions against
+// the same grid with the same reach (r < h), so its recorded row masks stand
+// in for phase 1; the body keeps its own j != i and r^2 > 1e-12 tests.
+template <bool EXACT, bool RECORDED>
 __device__ __forceinline__ float3 delta_sum_f(const SegParams &s, const DeviceState &d, const float4 *__restrict__ pred,
                                               int i, float4 pi)
 {
@@ -59,14 +63,19 @@ __device__ __forceinline__ float3 delta_sum_f(const SegParams &s, const DeviceSt
   const int3 base = cell_coord(s, pi.x, pi.y, pi.z);
   float ax = 0.0f, ay = 0.0f, az = 0.0f;
   const float h2 = s.h2;
-  for_each_within<EXACT>(s, d.offsets, pred, pi, h2, base, [&](int k) {
+  auto body = [&](int k) {
     if (k == i) return;
     const float4 pj = __ldg(&pred[k]);
     const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
     const float r2 = pair_r2<EXACT>(dx, dy, dz);
     if (r2 >= h2 || r2 <= 1e-12f) return;
     delta_pair<EXACT>(s, lambda_i, __ldg(&d.lam[k].y), dx, dy, dz, r2, ax, ay, az);
-  });
+  };
+  if (RECORDED)
+    for_each_within_recorded<EXACT>(s, d.offsets, pred, pi, h2, base, MaskRecord{d.row_masks, d.row_wide, d.n}, i,
+                                    body);
+  else
+    for_each_within<EXACT>(s, d.offsets, pred, pi, h2, base, body);
   return make_float3(ax, ay, az);
 }
 
@@ -77,7 +86,7 @@ __global__ void __launch_bounds__(512) k_delta_apply_f(DeviceState d, const floa
 {
   FLOWX_SLOT_PROLOGUE
   const float4 pi = pred_in[i];
-  const float3 a = delta_sum_f<EXACT>(s, d, pred_in, i, pi);
+  const float3 a = delta_sum_f<EXACT, true>(s, d, pred_in, i, pi);
   const float rest = s.rest;
   pred_out[i] = make_float4(pi.x + a.x / rest, pi.y + a.y / rest, pi.z + a.z / rest, 1.0f);
 }
@@ -239,7 +248,7 @@ __global__ void k_predict(DeviceState d, float4 *__restrict__ pred)
 __global__ void __launch_bounds__(512) k_delta(DeviceState d, const float4 *__restrict__ pred)
 {
   FLOWX_SLOT_PROLOGUE
-  const float3 a = delta_sum_f<true>(s, d, pred, i, pred[i]);
+  const float3 a = delta_sum_f<true, false>(s, d, pred, i, pred[i]);
   const float rest = s.rest;
   d.delta[i] = make_float4(a.x / rest, a.y / rest, a.z / rest, 0.0f);
 }
