@@ -245,9 +245,13 @@ void launch_lambda(const DeviceState &d, const float4 *pred, cudaStream_t st);
 // fused substep (exact = the reference's expressions, else re-associated)
 void launch_lambda_f(const DeviceState &d, const float4 *pred, bool exact, cudaStream_t st);
 void launch_delta_apply_f(const DeviceState &d, const float4 *pred_in, float4 *pred_out, bool exact, cudaStream_t st);
+// record / recorded: the XSPH pass leaves its row masks for the next
+// substep's normal pass (same positions, same grid, same reach), which may
+// then skip its candidate tests; the caller vouches that nothing changed
+// positions, grid or slot order in between.
 void launch_xsph_finalize_f(const DeviceState &d, const float4 *pred, const float4 *pos_in, float4 *pos_out,
-                            bool keep_delta, bool exact, cudaStream_t st);
-void launch_normal_f(const DeviceState &d, const float4 *pred, float4 *out, bool exact, cudaStream_t st);
+                            bool keep_delta, bool exact, bool record, cudaStream_t st);
+void launch_normal_f(const DeviceState &d, const float4 *pred, float4 *out, bool exact, bool recorded, cudaStream_t st);
 void launch_splat_segment(const DeviceState &d, int seg, const float *surface_lo, float spacing,
                           float kernel_radius, float mass, float rest, const int *dims, float *out,
                           cudaStream_t st);

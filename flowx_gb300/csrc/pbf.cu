@@ -72,8 +72,8 @@ __device__ __forceinline__ float3 delta_sum_f(const SegParams &s, const DeviceSt
     delta_pair<EXACT>(s, lambda_i, __ldg(&d.lam[k].y), dx, dy, dz, r2, ax, ay, az);
   };
   if (RECORDED)
-    for_each_within_recorded<EXACT>(s, d.offsets, pred, pi, h2, base, MaskRecord{d.row_masks, d.row_wide, d.n}, i,
-                                    body);
+    for_each_within_recorded<EXACT, false>(s, d.offsets, pred, pi, h2, base, MaskRecord{d.row_masks, d.row_wide, d.n},
+                                           i, body);
   else
     for_each_within<EXACT>(s, d.offsets, pred, pi, h2, base, body);
   return make_float3(ax, ay, az);
@@ -93,14 +93,16 @@ __global__ void __launch_bounds__(512) k_delta_apply_f(DeviceState d, const floa
 
 // sph_xsph.glsl:35-81: c * sum (m / rho_j) (v_j - v_i) W(r), neighbour
 // velocities from velj(k, pred_k).
+// record: leave the row masks for the next substep's normal pass, which
+// tests the same positions against this grid with the same reach.
 template <bool EXACT, class VelJ>
 __device__ __forceinline__ float3 xsph_sum_f(const SegParams &s, const DeviceState &d, const float4 *__restrict__ pred,
-                                             int i, float4 q, float3 vi, VelJ &&velj)
+                                             int i, float4 q, float3 vi, bool record, VelJ &&velj)
 {
   const int3 base = cell_coord(s, q.x, q.y, q.z);
   const float h2 = s.h2, mass = s.mass, poly6 = s.poly6;
   float ax = 0.0f, ay = 0.0f, az = 0.0f;
-  for_each_within<EXACT>(s, d.offsets, pred, q, h2, base, [&](int k) {
+  auto body = [&](int k) {
     if (k == i) return;
     const float4 pj = __ldg(&pred[k]);
     const float dx = q.x - pj.x, dy = q.y - pj.y, dz = q.z - pj.z;
@@ -121,7 +123,12 @@ __device__ __forceinline__ float3 xsph_sum_f(const SegParams &s, const DeviceSta
       ay = __fmaf_rn(wk, __fsub_rn(vj.y, vi.y), ay);
       az = __fmaf_rn(wk, __fsub_rn(vj.z, vi.z), az);
     }
-  });
+  };
+  if (record)
+    for_each_within_recording<EXACT>(s, d.offsets, pred, q, h2, base, MaskRecord{d.row_masks, d.row_wide, d.n}, i,
+                                     body);
+  else
+    for_each_within<EXACT>(s, d.offsets, pred, q, h2, base, body);
   const float c = s.visc;
   return make_float3(c * ax, c * ay, c * az);
 }
@@ -130,7 +137,8 @@ __device__ __forceinline__ float3 xsph_sum_f(const SegParams &s, const DeviceSta
 template <bool EXACT>
 __global__ void __launch_bounds__(512) k_xsph_finalize_f(DeviceState d, const float4 *__restrict__ pred,
                                                          const float4 *__restrict__ pos_in,
-                                                         float4 *__restrict__ pos_out, int keep_delta)
+                                                         float4 *__restrict__ pos_out, int keep_delta,
+                                                         int record)
 {
   FLOWX_SLOT_PROLOGUE
   const float dtc = s.dtc;
@@ -144,7 +152,7 @@ __global__ void __launch_bounds__(512) k_xsph_finalize_f(DeviceState d, const fl
     vi = make_float3(__fmul_rn(__fsub_rn(q.x, p0.x), inv_dtc), __fmul_rn(__fsub_rn(q.y, p0.y), inv_dtc),
                      __fmul_rn(__fsub_rn(q.z, p0.z), inv_dtc));
   }
-  const float3 dv = xsph_sum_f<EXACT>(s, d, pred, i, q, vi, [&](int k, const float4 &pj) {
+  const float3 dv = xsph_sum_f<EXACT>(s, d, pred, i, q, vi, record != 0, [&](int k, const float4 &pj) {
     const float4 pk = __ldg(&pos_in[k]);
     if (EXACT) return slot_velocity(pj, pk, dtc);
     return make_float3(__fmul_rn(__fsub_rn(pj.x, pk.x), inv_dtc), __fmul_rn(__fsub_rn(pj.y, pk.y), inv_dtc),
@@ -159,16 +167,18 @@ __global__ void __launch_bounds__(512) k_xsph_finalize_f(DeviceState d, const fl
 }
 
 // sph_normal.glsl:24-81 (over the previous substep's grid, as the reference).
+// recorded: the previous substep's XSPH pass left its row masks for these
+// positions, this grid and this reach.
 template <bool EXACT>
 __global__ void __launch_bounds__(512) k_normal_f(DeviceState d, const float4 *__restrict__ pred,
-                                                  float4 *__restrict__ out)
+                                                  float4 *__restrict__ out, int recorded)
 {
   FLOWX_SLOT_PROLOGUE
   const float4 pi = pred[i];
   const int3 base = cell_coord(s, pi.x, pi.y, pi.z);
   const float h = s.h, h2 = s.h2, mass = s.mass, poly6m6 = s.poly6m6, vlap = s.visclap;
   float nx = 0.0f, ny = 0.0f, nz = 0.0f, lap = 0.0f;
-  for_each_within<EXACT>(s, d.offsets, pred, pi, h2, base, [&](int k) {
+  auto body = [&](int k) {
     if (k == i) return;
     const float4 pj = __ldg(&pred[k]);
     const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
@@ -195,7 +205,12 @@ __global__ void __launch_bounds__(512) k_normal_f(DeviceState d, const float4 *_
       const float r = r2 > 0.0f ? __fmul_rn(r2, rsqrtf(r2)) : 0.0f;
       lap = __fmaf_rn(__fmul_rn(weight, vlap), __fsub_rn(h, r), lap);
     }
-  });
+  };
+  if (recorded)
+    for_each_within_recorded<EXACT, true>(s, d.offsets, pred, pi, h2, base, MaskRecord{d.row_masks, d.row_wide, d.n},
+                                          i, body);
+  else
+    for_each_within<EXACT>(s, d.offsets, pred, pi, h2, base, body);
   const float mag = sqrtf(nx * nx + ny * ny + nz * nz);
   const float curv = (mag > 1e-4f) ? -lap / mag : 0.0f;
   out[i] = make_float4(nx, ny, nz, curv);
@@ -217,20 +232,21 @@ void launch_delta_apply_f(const DeviceState &d, const float4 *pred_in, float4 *p
   else k_delta_apply_f<false><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred_in, pred_out);
 }
 void launch_xsph_finalize_f(const DeviceState &d, const float4 *pred, const float4 *pos_in, float4 *pos_out,
-                            bool keep_delta, bool exact, cudaStream_t st)
+                            bool keep_delta, bool exact, bool record, cudaStream_t st)
 {
   const int b = FLOWX_BLOCK(d, K_XSPH_FINALIZE, 128,
                             exact ? (const void *)k_xsph_finalize_f<true> : (const void *)k_xsph_finalize_f<false>);
   if (d.n <= 0) return;
-  if (exact) k_xsph_finalize_f<true><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred, pos_in, pos_out, keep_delta);
-  else k_xsph_finalize_f<false><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred, pos_in, pos_out, keep_delta);
+  const size_t sm = row_mask_bytes(b);
+  if (exact) k_xsph_finalize_f<true><<<grid_for(d.n, b), b, sm, st>>>(d, pred, pos_in, pos_out, keep_delta, record);
+  else k_xsph_finalize_f<false><<<grid_for(d.n, b), b, sm, st>>>(d, pred, pos_in, pos_out, keep_delta, record);
 }
-void launch_normal_f(const DeviceState &d, const float4 *pred, float4 *out, bool exact, cudaStream_t st)
+void launch_normal_f(const DeviceState &d, const float4 *pred, float4 *out, bool exact, bool recorded, cudaStream_t st)
 {
   const int b = FLOWX_BLOCK(d, K_NORMAL, 128, exact ? (const void *)k_normal_f<true> : (const void *)k_normal_f<false>);
   if (d.n <= 0) return;
-  if (exact) k_normal_f<true><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred, out);
-  else k_normal_f<false><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred, out);
+  if (exact) k_normal_f<true><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred, out, recorded);
+  else k_normal_f<false><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred, out, recorded);
 }
 
 // ---- single reference passes (per-pass API; always exact) ------------------
@@ -273,7 +289,7 @@ __global__ void __launch_bounds__(512) k_xsph(DeviceState d, const float4 *__res
   FLOWX_SLOT_PROLOGUE
   const float4 vi4 = d.vel[i];
   const float4 *__restrict__ vel = d.vel;
-  const float3 dv = xsph_sum_f<true>(s, d, pred, i, pred[i], make_float3(vi4.x, vi4.y, vi4.z),
+  const float3 dv = xsph_sum_f<true>(s, d, pred, i, pred[i], make_float3(vi4.x, vi4.y, vi4.z), false,
                                      [&](int k, const float4 &) {
                                        const float4 v = __ldg(&vel[k]);
                                        return make_float3(v.x, v.y, v.z);
@@ -294,7 +310,7 @@ __global__ void k_finalize(DeviceState d, const float4 *__restrict__ pred)
 
 void launch_normal(const DeviceState &d, const float4 *pred, float4 *out, cudaStream_t st)
 {
-  launch_normal_f(d, pred, out, true, st);
+  launch_normal_f(d, pred, out, true, false, st);
 }
 void launch_lambda(const DeviceState &d, const float4 *pred, cudaStream_t st) { launch_lambda_f(d, pred, true, st); }
 void launch_predict(const DeviceState &d, float4 *pred, cudaStream_t st)

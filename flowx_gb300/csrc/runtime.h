@@ -16,8 +16,9 @@ extern std::atomic<long long> g_launches;
 float bits_to_float(int32_t b);
 void seg_from_push(const flowx_push &p, SegParams &s);
 
-// (iterations, substeps, starting predicted buffer, cells, normal pass on, flags)
-using GraphKey = std::tuple<int, int, int, int, int, int>;
+// (iterations, substeps, starting predicted buffer, cells, normal pass on, flags,
+// first normal pass reuses the previous XSPH masks)
+using GraphKey = std::tuple<int, int, int, int, int, int, int>;
 struct GraphEntry {
   cudaGraphExec_t exec = nullptr;
   long long kernels = 0;
@@ -50,6 +51,8 @@ struct Ctx {
   bool normal_zero = true;         // normal holds only the zeros it was created with
   bool normal_in_order = true;     // normal / delta still follow the slot order
   bool delta_in_order = true;
+  bool xsph_masks_valid = false;   // the last fused substep's XSPH row masks still describe
+                                   // pred_cur() against the current grid and reach
   int collider_dims[3] = {0, 0, 0};
   std::string err;
   std::map<GraphKey, GraphEntry> graphs;
@@ -66,7 +69,7 @@ struct Ctx {
   int upload_segs(const std::vector<SegParams> &s, int cells);
   void issue_build_from_pred(const float4 *pred);
   int build_grid_generic();
-  int issue_substep(int iterations, int pred_in_idx);
+  int issue_substep(int iterations, int pred_in_idx, bool normal_recorded);
   bool segs_need_normal() const;
   void after_fused_substep();
   int ensure_grid();
