@@ -171,6 +171,15 @@ def load(path: str | None = None):
         "flowx_adjoint_forward": ([vp, P(Push), ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, P(Push), vp],
                                   ctypes.c_int),
         "flowx_substep_adjoint": ([vp, vp, vp, vp, vp, vp], ctypes.c_int),
+        "flowx_mc_create": ([ctypes.c_int32, P(vp)], ctypes.c_int),
+        "flowx_mc_destroy": ([vp], ctypes.c_int),
+        "flowx_mc_last_error": ([vp], ctypes.c_char_p),
+        "flowx_mc_extract": ([vp, vp, P(ctypes.c_int32), P(ctypes.c_double), ctypes.c_double, ctypes.c_double, vp,
+                              P(ctypes.c_int64), P(ctypes.c_int64)], ctypes.c_int),
+        "flowx_mc_download": ([vp, vp, ctypes.c_size_t, vp, ctypes.c_size_t], ctypes.c_int),
+        "flowx_mc_mesh": ([vp, P(vp), P(vp)], ctypes.c_int),
+        "flowx_mc_case_table": ([ctypes.c_int32, P(ctypes.c_int32), P(ctypes.c_int32)], ctypes.c_int),
+        "flowx_surface_field": ([ctx, P(vp), P(ctypes.c_int64)], ctypes.c_int),
         "flowx_build_grid_static": ([vp, ctypes.c_int32, P(Push), vp, ctypes.c_int32, vp, vp, vp], ctypes.c_int),
         "flowx_build_grid_static_error": ([], ctypes.c_char_p),
     }

@@ -133,6 +133,15 @@ static int fetch_ids_keys(Ctx *c, std::vector<uint32_t> &ids, std::vector<uint32
 
 extern "C" {
 
+int flowx_surface_field(flowx_ctx *ctx, const float **field, int64_t *samples)
+{
+  if (!ctx || !field || !samples) return FLOWX_ERR_ARG;
+  Ctx *c = reinterpret_cast<Ctx *>(ctx);
+  *field = c->d.surface;
+  *samples = c->cap_samples;
+  return FLOWX_OK;
+}
+
 int flowx_upload(flowx_ctx *ctx, int buffer, const void *host, size_t bytes)
 {
   if (!ctx) return FLOWX_ERR_ARG;

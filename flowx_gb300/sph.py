@@ -80,6 +80,7 @@ class Solver:
         cfg.max_collider_voxels = int(max_collider_voxels if max_collider_voxels is not None else vox)
         cfg.max_surface_samples = int(max_surface_samples)
         cfg.device = int(device)
+        self.config_device = int(device)
         cfg.flags = (_lib.FLAG_KEEP_DELTA if keep_delta else 0) | (_lib.FLAG_EXACT if exact else 0)
         check(self.lib.flowx_create(ctypes.byref(cfg), ctypes.byref(self._ctx)))
         self.collider_dims = None
@@ -232,6 +233,19 @@ class Solver:
             return out
         check(self.lib.flowx_splat(self._ctx, ctypes.byref(push), None, 0), self._ctx)
         return None
+
+    def surface_mesh(self, surface: SurfaceConfig, dt=0.0, mc=None):
+        """The per-frame surface (solver/surface.py:201-244): splat, then marching
+        cubes on the device; returns (vertices V x 3 float64, triangles T x 3 int32)."""
+        from .surface import MarchingCubes
+
+        self.update_surface(surface, dt, download=False)
+        field = ctypes.c_void_p()
+        samples = ctypes.c_int64()
+        check(self.lib.flowx_surface_field(self._ctx, ctypes.byref(field), ctypes.byref(samples)), self._ctx)
+        mc = mc or MarchingCubes(self.config_device)
+        mc.extract_device(field.value, surface.dims, surface.lo, surface.spacing, surface.iso, self.stream())
+        return mc.download()
 
     def synchronize(self):
         check(self.lib.flowx_synchronize(self._ctx), self._ctx)

@@ -307,6 +307,34 @@ int flowx_adjoint_forward(flowx_adjoint *adj, const flowx_push *push, int iterat
 int flowx_substep_adjoint(flowx_adjoint *adj, const float *surface_grad, const float *positions_out_grad,
                           const float *velocities_out_grad, float *positions_grad, float *velocities_grad);
 
+/* ---- Marching cubes (solver/marching_cubes.py:191-280, extract) ----------
+ * Iso-surface of a float32 lattice field on the device (x fastest, sample
+ * (i, j, k) at origin + (i, j, k) * spacing, inside where value >= iso), as
+ * the reference's indexed mesh: the same vertices in the same order with the
+ * same float64 coordinates, and the same triangles. The object owns its
+ * device scratch and mesh buffers (grown as needed). */
+typedef struct flowx_mc flowx_mc;
+
+int flowx_mc_create(int32_t device, flowx_mc **out);
+int flowx_mc_destroy(flowx_mc *mc);
+const char *flowx_mc_last_error(const flowx_mc *mc);
+/* Extract on `stream` (NULL = default stream; it is synchronised for the
+ * counts). field: device pointer, dims[0] * dims[1] * dims[2] floats. */
+int flowx_mc_extract(flowx_mc *mc, const float *field, const int32_t dims[3], const double origin[3], double spacing,
+                     double iso, void *stream, int64_t *vertex_count, int64_t *triangle_count);
+/* The last extraction to host: vertices V x 3 doubles, triangles T x 3 int32. */
+int flowx_mc_download(flowx_mc *mc, double *vertices, size_t vertex_bytes, int32_t *triangles,
+                      size_t triangle_bytes);
+/* Device pointers to the last extraction's mesh (valid until the next extract). */
+int flowx_mc_mesh(flowx_mc *mc, const double **vertices, const int32_t **triangles);
+/* The derived case table (no GPU needed): triangle_count triangles of edge
+ * indices for corner-sign case mc_case (bit c = corner c inside); edges must
+ * hold 15 ints. */
+int flowx_mc_case_table(int32_t mc_case, int32_t *edges, int32_t *triangle_count);
+/* The context's splat grid on the device (after flowx_splat), for
+ * flowx_mc_extract: the pointer and its capacity in samples. */
+int flowx_surface_field(flowx_ctx *ctx, const float **field, int64_t *samples);
+
 /* Grid build that allocates nothing. There is no counterpart in the
  * reference: its grid build (solver/sph.py:482-498) always runs inside a
  * context that owns its buffers.
