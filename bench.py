@@ -515,6 +515,19 @@ def run_flowx(args):
     s1.record(stream)
     s1.synchronize()
     splat_ms = s0.elapsed_time(s1) / reps
+    # ---- per-frame surface mesh: splat + marching cubes on the device ----
+    from flowx_gb300.surface import MarchingCubes
+
+    mc = MarchingCubes(0)
+    sol.surface_mesh(scene.surface, dt, mc)
+    m0 = time.perf_counter()
+    for _ in range(reps):
+        verts, tris = sol.surface_mesh(scene.surface, dt, mc)
+    mesh_ms = (time.perf_counter() - m0) / reps * 1e3
+    surface_mesh = {"ms_per_frame": mesh_ms, "vertices": int(verts.shape[0]), "triangles": int(tris.shape[0]),
+                    "samples": int(scene.surface.sample_count),
+                    "timing": "wall clock of Solver.surface_mesh: splat, marching cubes and the mesh download"}
+    mc.close()
     finite = bool(np.isfinite(pinned_pos).all())
     sol.close()
 
@@ -558,6 +571,7 @@ def run_flowx(args):
             "batched": batched,
             "adjoint": adjoint,
             "splat_ms_per_frame": splat_ms,
+            "surface_mesh": surface_mesh,
             "splat_samples": samples,
             "state_finite": finite,
         }
