@@ -106,6 +106,21 @@ class AdjointConfig(ctypes.Structure):
     ]
 
 
+class CacheHeader(ctypes.Structure):
+    """flowx_cache_header (include/flowx.h)."""
+
+    _fields_ = [
+        ("flowx_version", ctypes.c_char * 16),
+        ("particle_count", ctypes.c_int32),
+        ("seed_frame", ctypes.c_int32),
+        ("last_frame", ctypes.c_int32),
+        ("fps", ctypes.c_float),
+        ("collider_count", ctypes.c_int32),
+        ("collider_names", ctypes.POINTER(ctypes.c_char_p)),
+        ("config_hash", ctypes.c_uint8 * 32),
+    ]
+
+
 class FlowxError(RuntimeError):
     def __init__(self, code, message):
         super().__init__(f"{ERRORS.get(code, code)}: {message}")
@@ -180,6 +195,16 @@ def load(path: str | None = None):
         "flowx_mc_mesh": ([vp, P(vp), P(vp)], ctypes.c_int),
         "flowx_mc_case_table": ([ctypes.c_int32, P(ctypes.c_int32), P(ctypes.c_int32)], ctypes.c_int),
         "flowx_surface_field": ([ctx, P(vp), P(ctypes.c_int64)], ctypes.c_int),
+        "flowx_cache_create": ([ctypes.c_char_p, P(CacheHeader), P(vp)], ctypes.c_int),
+        "flowx_cache_open": ([ctypes.c_char_p, P(vp)], ctypes.c_int),
+        "flowx_cache_close": ([vp], ctypes.c_int),
+        "flowx_cache_last_error": ([vp], ctypes.c_char_p),
+        "flowx_cache_info": ([vp, P(CacheHeader)], ctypes.c_int),
+        "flowx_cache_collider_name": ([vp, ctypes.c_int32], ctypes.c_char_p),
+        "flowx_cache_write_frame": ([vp, ctx, ctypes.c_int32], ctypes.c_int),
+        "flowx_cache_load_frame": ([vp, ctx, ctypes.c_int32, P(Push)], ctypes.c_int),
+        "flowx_cache_write_frame_host": ([vp, ctypes.c_int32, vp, vp], ctypes.c_int),
+        "flowx_cache_read_frame_host": ([vp, ctypes.c_int32, vp, vp], ctypes.c_int),
         "flowx_build_grid_static": ([vp, ctypes.c_int32, P(Push), vp, ctypes.c_int32, vp, vp, vp], ctypes.c_int),
         "flowx_build_grid_static_error": ([], ctypes.c_char_p),
     }

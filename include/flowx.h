@@ -335,6 +335,45 @@ int flowx_mc_case_table(int32_t mc_case, int32_t *edges, int32_t *triangle_count
  * flowx_mc_extract: the pointer and its capacity in samples. */
 int flowx_surface_field(flowx_ctx *ctx, const float **field, int64_t *samples);
 
+/* ---- Disk cache (solver/cache.py, format FLWXCA01 version 2) -------------
+ * Per-frame (positions, velocities) snapshots in the reference's file layout
+ * (header, then frames seed_frame + 1 .. last_frame of N x 4 f32 positions
+ * and N x 4 f32 velocities at arithmetic offsets; last_frame rewritten after
+ * every frame write). Which file to trust (config hash, collider names) is
+ * the host's decision, as in the reference; these calls read and write. */
+typedef struct flowx_cache flowx_cache;
+
+typedef struct flowx_cache_header {
+  char flowx_version[16];        /* NUL padded */
+  int32_t particle_count;
+  int32_t seed_frame;
+  int32_t last_frame;            /* output of flowx_cache_info; create sets it to seed_frame */
+  float fps;
+  int32_t collider_count;
+  const char *const *collider_names;  /* create: collider_count names; info: NULL (see below) */
+  uint8_t config_hash[32];       /* sha256 of the run's settings */
+} flowx_cache_header;
+
+/* A new file (truncated) holding only the header. */
+int flowx_cache_create(const char *path, const flowx_cache_header *header, flowx_cache **out);
+/* An existing file; FLOWX_ERR_ARG when it is not a version-2 FLWXCA01 file. */
+int flowx_cache_open(const char *path, flowx_cache **out);
+int flowx_cache_close(flowx_cache *cache);
+const char *flowx_cache_last_error(const flowx_cache *cache);
+int flowx_cache_info(const flowx_cache *cache, flowx_cache_header *header);
+const char *flowx_cache_collider_name(const flowx_cache *cache, int32_t index);
+/* solver/cache.py:339-379: store a context's positions and velocities (id
+ * order) as `frame`; frames at or before the seed frame are not stored. */
+int flowx_cache_write_frame(flowx_cache *cache, flowx_ctx *ctx, int32_t frame);
+/* solver/cache.py:382-421 + solver/sph.py:700-733: install a cached frame in
+ * the context (positions, velocities, predicted = positions, lambda zero, the
+ * grid rebuilt with `push`). FLOWX_ERR_ARG outside seed_frame < frame <=
+ * last_frame. */
+int flowx_cache_load_frame(flowx_cache *cache, flowx_ctx *ctx, int32_t frame, const flowx_push *push);
+/* The same with host arrays (N x 4 floats each), no device involved. */
+int flowx_cache_write_frame_host(flowx_cache *cache, int32_t frame, const float *positions, const float *velocities);
+int flowx_cache_read_frame_host(flowx_cache *cache, int32_t frame, float *positions, float *velocities);
+
 /* Grid build that allocates nothing. There is no counterpart in the
  * reference: its grid build (solver/sph.py:482-498) always runs inside a
  * context that owns its buffers.
