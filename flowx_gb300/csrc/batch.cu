@@ -229,9 +229,10 @@ int flowx_batch_splat(flowx_ctx *ctx, int scene, const flowx_push *splat_push, f
   if (rc) return rc;
   rc = c->ensure_grid();
   if (rc) return rc;
-  launch_splat_segment(c->d, scene, splat_push->f_hi, bits_to_float(splat_push->i_sort[3]), splat_push->f_sph[0],
-                       splat_push->f_sph[1], splat_push->f_sph[2], dims, c->d.surface, c->stream);
-  g_launches += 1;
+  launch_splat_segment(c->d, scene, c->segs[scene].c_begin, c->segs[scene].c_count, splat_push->f_hi,
+                       bits_to_float(splat_push->i_sort[3]), splat_push->f_sph[0], splat_push->f_sph[1],
+                       splat_push->f_sph[2], dims, c->d.surface, c->stream);
+  g_launches += 2;
   rc = c->check_launch("flowx_batch_splat");
   if (rc) return rc;
   if (host_out) {

@@ -392,9 +392,9 @@ int flowx_splat(flowx_ctx *ctx, const flowx_push *push, float *host_out, size_t 
   rc = c->ensure_offsets();
   if (rc) return rc;
   if (!c->have_grid) return c->fail(FLOWX_ERR_STATE, "splat before any grid build");
-  launch_splat_segment(c->d, 0, push->f_hi, bits_to_float(push->i_sort[3]), push->f_sph[0], push->f_sph[1],
-                       push->f_sph[2], dims, c->d.surface, c->stream);
-  g_launches += 1;
+  launch_splat_segment(c->d, 0, c->segs[0].c_begin, c->segs[0].c_count, push->f_hi, bits_to_float(push->i_sort[3]),
+                       push->f_sph[0], push->f_sph[1], push->f_sph[2], dims, c->d.surface, c->stream);
+  g_launches += 2;
   rc = c->check_launch("flowx_splat");
   if (rc) return rc;
   if (host_out) {

