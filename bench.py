@@ -137,6 +137,25 @@ def _dist():
     return world, rank, local
 
 
+def _max_over_ranks(value: float, world: int, device="cpu") -> float:
+    """The largest of every rank's value (the replica timing rule: the job
+    takes as long as its slowest rank); the value itself for one rank."""
+    if world <= 1:
+        return float(value)
+    import torch
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _replica_throughput(particles: int, substeps_per_step: int, steps: int, world: int, seconds: float) -> float:
+    """Whole-job particle-substeps/s of ``world`` independent replicas that each
+    advanced ``particles`` particles by ``steps`` x ``substeps_per_step``
+    substeps in ``seconds`` (the max over ranks)."""
+    return particles * substeps_per_step * steps * world / seconds
+
+
 def _workload(args):
     from flowx_gb300 import scenes
 
@@ -427,11 +446,8 @@ def run_flowx(args):
     ms = e0.elapsed_time(e1)
     launches = launch_count() - launches0
     clocks.stop()
-    if world > 1:
-        t = torch.tensor([ms], device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = scene.n * nsub * args.steps * world / (ms / 1e3)
+    ms = _max_over_ranks(ms, world, f"cuda:{local}")
+    value = _replica_throughput(scene.n, nsub, args.steps, world, ms / 1e3)
 
     # ---- per-kernel times (launch by launch, same state and stream) ----
     prof = sol.profile(dt, nsub * min(args.steps, 4))
@@ -492,12 +508,9 @@ def run_flowx(args):
                                           pinned_pos.nbytes), sol.ctx)
     sol.synchronize()
     e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = _max_over_ranks(e2e_s, world, f"cuda:{local}")
     e2e = {
-        "value": scene.n * nsub * args.steps * world / e2e_s,
+        "value": _replica_throughput(scene.n, nsub, args.steps, world, e2e_s),
         "unit": UNIT,
         "h2d_bytes_per_step": int(np.prod(dims)) if dims is not None else 0,
         "d2h_bytes_per_step": int(scene.n * 16),
