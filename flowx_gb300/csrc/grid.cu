@@ -258,13 +258,15 @@ __global__ void k_cell_sort_small(DeviceState d)
 
 // Large cells (listed by the scan): a block ranks each element against all
 // others of its cell (ids are unique, so ranks are a permutation), writes to
-// the scratch copy and copies back. O(n^2 / blockDim) per cell.
+// the scratch copy and copies back. O(n^2 / blockDim) per cell, so cells
+// above kMaxRankSortCell are left in the scatter's order.
 __global__ void __launch_bounds__(256) k_cell_sort_large(DeviceState d)
 {
   const uint32_t count = d.big_cells[0];
   for (uint32_t item = blockIdx.x; item < count; item += gridDim.x) {
     const uint32_t c = d.big_cells[1 + item];
     const uint32_t a = d.offsets[c], n = d.offsets[c + 1] - a;
+    if (n > (uint32_t)kMaxRankSortCell) continue;  // uniform across the block
     for (uint32_t e = threadIdx.x; e < n; e += blockDim.x) {
       const unsigned long long mine = d.pairs[a + e];
       uint32_t rank = 0;
