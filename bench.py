@@ -280,6 +280,30 @@ def _batched_metrics(substeps=20, warmup=3):
     }
 
 
+def _other_configs(frames=10, warmup=3):
+    """The other plain configurations (particle-substeps/s, device-resident,
+    CUDA events around ``frames`` graph-launched frames of 4 substeps after
+    ``warmup``): the 3,200-particle dam break and the 307,200-particle pool
+    with its colliders."""
+    from flowx_gb300 import scenes
+    from flowx_gb300.sph import Solver
+
+    out = {}
+    for name in ("dam_break", "pool"):
+        sc = getattr(scenes, name)()
+        col = sc.collider_grid(0)
+        with Solver(sc.config, sc.positions, sc.velocities, collider=col,
+                    collider_voxel=sc.collider_voxel if col is not None else 0.0) as s:
+            s._build_grid(0.0)
+            for _ in range(warmup):
+                s.step_substeps(sc.dt, sc.substeps_per_frame)
+            s.synchronize()
+            ms = s.time_steps(sc.dt, sc.substeps_per_frame, frames)
+        out[name] = {"particles": sc.n, "value": sc.n * sc.substeps_per_frame * frames / (ms / 1e3),
+                     "unit": UNIT, "ms_per_frame": ms / frames}
+    return out
+
+
 def _adjoint_metrics(adam_steps=200, repeats=5):
     """The differentiable workload (20,000 particles in a 1 m cube, h 0.04,
     initial velocities from a 3x3x3 control grid of 3-vectors, loss = squared
@@ -471,6 +495,10 @@ def run_flowx(args):
     if os.path.exists(traffic_path):
         with open(traffic_path) as f:
             traffic = json.load(f).get("bytes_per_launch", {}).get(dominant)
+    warp_inst = None
+    if os.path.exists(traffic_path):
+        with open(traffic_path) as f:
+            warp_inst = json.load(f).get("warp_instructions_per_launch", {}).get(dominant)
     roofline = {
         "bound": "hbm",
         "kernel": dominant,
@@ -550,6 +578,7 @@ def run_flowx(args):
     adjoint = None
     if rank == 0 and not args.no_adjoint:
         adjoint = _adjoint_metrics()
+    other_configs = _other_configs() if rank == 0 else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -559,6 +588,20 @@ def run_flowx(args):
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {exc}"}
 
     if rank == 0:
+        clock_summary = clocks.summary()
+        issue_roofline = None
+        if warp_inst and clock_summary.get("sm_max_mhz"):
+            # The neighbour kernels are instruction-issue-bound: their warp
+            # instructions per launch (ncu, profiles/traffic.json) over the live
+            # time per launch, against 4 issue slots per SM per cycle at the
+            # maximum SM clock.
+            sms = torch.cuda.get_device_properties(local).multi_processor_count
+            peak_issue = 4.0 * sms * clock_summary["sm_max_mhz"] * 1e6
+            achieved_issue = warp_inst / (dom_ms * 1e-3)
+            issue_roofline = {"kernel": dominant, "warp_instructions_per_launch": warp_inst,
+                              "ms_per_launch": dom_ms, "achieved": achieved_issue, "peak": peak_issue,
+                              "unit": "warp-instructions/s", "frac": achieved_issue / peak_issue,
+                              "peak_basis": f"4 x {sms} SMs x {clock_summary['sm_max_mhz']:.0f} MHz"}
         line = {
             "metric": METRIC,
             "value": value,
@@ -578,11 +621,13 @@ def run_flowx(args):
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": int(launches),
-            "clocks": clocks.summary(),
+            "clocks": clock_summary,
+            "issue_roofline": issue_roofline,
             "kernels": kernels,
             "math": "fast (re-associated float32; FLOWX_FLAG_EXACT gives the reference's expressions)",
             "batched": batched,
             "adjoint": adjoint,
+            "other_configs": other_configs,
             "splat_ms_per_frame": splat_ms,
             "surface_mesh": surface_mesh,
             "splat_samples": samples,
