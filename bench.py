@@ -31,6 +31,7 @@ the sum of all replicas' particle-substeps ("replicas only", weak scaling).
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import json
 import os
 import statistics
@@ -215,7 +216,55 @@ def _oracle_sample(scene, target_s=10.0, max_substeps=4):
         "kind": "port",
         "sample": f"{done} substep(s) of the full {scene.n}-particle workload from its seeded state "
                   f"({elapsed:.1f} s, oracle C restatement, OpenMP {cores} threads, stable grid order)",
+        "one_core": _oracle_one_core(scene, cores),
     }
+
+
+def _oracle_one_core(scene, restore_threads, corner=0.25):
+    """The oracle on one host thread: one substep of the particles of the
+    workload's seeded state whose x and y lie in the lowest ``corner`` of the
+    domain (a full-height column of the same fluid, same cells and
+    parameters), as particle-substeps/s."""
+    from flowx_gb300 import config as C
+    from oracle import oracle as O
+
+    c = scene.config
+    lo = np.asarray(c.lo, np.float32)
+    ext = np.asarray(c.hi, np.float32) - lo
+    keep = ((scene.positions[:, 0] - lo[0] < corner * ext[0]) & (scene.positions[:, 1] - lo[1] < corner * ext[1]))
+    pos = np.ascontiguousarray(scene.positions[keep])
+    vel = np.ascontiguousarray(scene.velocities[keep])
+    n = int(pos.shape[0])
+    cfg = dataclasses.replace(c, particle_count=n)
+    ic = C.collider_binding(scene.collider_dims, scene.collider_voxel)
+    o = O.Oracle(C.push_constant_values(cfg, scene.dt, ic), pos, vel, collider=scene.collider_grid(0),
+                 iterations=c.iterations)
+    o.build_grid(0.0, order=O.ORDER_STABLE)
+    O.set_threads(1)
+    try:
+        t0 = time.perf_counter()
+        o.substep(scene.dt, order=O.ORDER_STABLE)
+        elapsed = time.perf_counter() - t0
+    finally:
+        O.set_threads(restore_threads)
+    return {"value": n / elapsed, "unit": UNIT, "cores": 1,
+            "sample": f"one substep of the {n} particles of the seeded state in the x, y < {corner:g} x extent "
+                      f"column ({elapsed:.1f} s, oracle C restatement, one thread)"}
+
+
+def _oracle_extract(field, surface, verts, tris):
+    """The oracle's marching cubes (NumPy restatement of the reference's
+    extract, one thread) on the frame's splat grid, timed, and whether the
+    device mesh equals its mesh."""
+    from oracle import mc as oracle_mc
+
+    t0 = time.perf_counter()
+    v, t = oracle_mc.extract(field, surface.dims, surface.lo, surface.spacing, surface.iso)
+    elapsed = time.perf_counter() - t0
+    return {"ms": elapsed * 1e3, "cores": 1, "kind": "port",
+            "matches_device": bool(np.array_equal(v, verts) and np.array_equal(t, tris)),
+            "sample": "one extraction of the frame's splat grid (oracle NumPy restatement of the reference's "
+                      "marching cubes; the reference's own is a pure-Python loop)"}
 
 
 def _batched_metrics(substeps=20, warmup=3):
@@ -568,6 +617,9 @@ def run_flowx(args):
     surface_mesh = {"ms_per_frame": mesh_ms, "vertices": int(verts.shape[0]), "triangles": int(tris.shape[0]),
                     "samples": int(scene.surface.sample_count),
                     "timing": "wall clock of Solver.surface_mesh: splat, marching cubes and the mesh download"}
+    if rank == 0 and not args.no_cpu_baseline:
+        surface_mesh["cpu_extract"] = _oracle_extract(sol.update_surface(scene.surface, dt), scene.surface,
+                                                      verts, tris)
     mc.close()
     finite = bool(np.isfinite(pinned_pos).all())
     sol.close()

@@ -82,3 +82,54 @@ def test_solver_surface_mesh_matches_reference_on_oracle_splat():
         verts, tris = s.surface_mesh(sc.surface, sc.dt)
     np.testing.assert_array_equal(tris, z["splat_triangles"])
     np.testing.assert_array_equal(verts, z["splat_vertices"])
+
+
+def _smooth_field(dims, seed):
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = dims
+    z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    f = np.zeros((nz, ny, nx), np.float64)
+    for _ in range(6):
+        k = rng.uniform(0.02, 0.12, 3)
+        ph = rng.uniform(0, 2 * np.pi, 3)
+        f += np.sin(k[0] * x + ph[0]) * np.sin(k[1] * y + ph[1]) * np.sin(k[2] * z + ph[2])
+    return f.astype(np.float32).reshape(-1)
+
+
+@pytest.mark.parametrize("dims,iso", [((192, 160, 144), 0.0), ((97, 131, 64), 0.35)])
+def test_extract_matches_oracle_beyond_fixtures(dims, iso):
+    """Lattices larger and more ragged than the fixtures: the device mesh
+    equals the oracle's (oracle/mc.py, itself pinned to the reference's
+    meshes), vertices bit-identical."""
+    from flowx_gb300.surface import MarchingCubes
+    from oracle import mc as oracle_mc
+
+    field = _smooth_field(dims, seed=sum(dims))
+    mc = MarchingCubes(0)
+    verts, tris = mc.extract(field, dims, (-0.3, 0.1, 0.7), 0.0123, iso)
+    ov, ot = oracle_mc.extract(field, dims, (-0.3, 0.1, 0.7), 0.0123, iso)
+    assert len(ot) > 10000
+    np.testing.assert_array_equal(tris, ot)
+    np.testing.assert_array_equal(verts, ov)
+    mc.close()
+
+
+def test_solver_surface_mesh_matches_oracle_pool():
+    """The 307,200-particle pool scene after two substeps: the device mesh of
+    its 128^3 splat equals the oracle's mesh of the same splat grid."""
+    from flowx_gb300 import scenes
+    from flowx_gb300.sph import Solver
+    from oracle import mc as oracle_mc
+
+    sc = scenes.pool()
+    with Solver(sc.config, sc.positions, sc.velocities, collider=sc.collider_grid(0),
+                collider_voxel=sc.collider_voxel, max_surface_samples=sc.surface.sample_count) as s:
+        s._build_grid(0.0)
+        for _ in range(2):
+            s._substep(sc.dt)
+        verts, tris = s.surface_mesh(sc.surface, sc.dt)
+        field = s.update_surface(sc.surface, sc.dt)
+    ov, ot = oracle_mc.extract(field, sc.surface.dims, sc.surface.lo, sc.surface.spacing, sc.surface.iso)
+    assert len(ot) > 10000
+    np.testing.assert_array_equal(tris, ot)
+    np.testing.assert_array_equal(verts, ov)
