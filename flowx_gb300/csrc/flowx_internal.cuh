@@ -109,6 +109,24 @@ int kernel_max_threads(const void *kernel);
   }())
 
 // Device pointers of one context's state (all in grid order).
+// Predicted positions of four consecutive slots, coordinate-major (slot
+// 4g + u in lane u of x, y and z): the candidate filter of the neighbour
+// passes reads four candidates with three 16-byte loads and tests them two
+// at a time with paired float arithmetic.
+struct SlotQuad {
+  float4 x, y, z;
+};
+
+// Slot k's predicted position into its lane of the slot quads.
+__device__ __forceinline__ void store_quad(SlotQuad *__restrict__ quads, int k, float x, float y, float z)
+{
+  float *g = reinterpret_cast<float *>(quads + (k >> 2));
+  const int u = k & 3;
+  g[u] = x;
+  g[4 + u] = y;
+  g[8 + u] = z;
+}
+
 struct DeviceState {
   int block[K_COUNT];       // block size per kernel, 0 = the kernel's default
   float4 *pos, *pos_alt;    // positions; pos_alt receives the permuted copy
@@ -130,6 +148,8 @@ struct DeviceState {
   float4 *cell_lo, *cell_hi;  // per cell: bounds of its particles' positions (the splat's cell test)
   unsigned long long *row_masks;  // the lambda pass's neighbour masks, 9 per slot (row-major)
   uint8_t *row_wide;        // per slot: masks not recorded (a row over 64 slots)
+  SlotQuad *quads;          // ceil(n / 4) groups: the predicted positions the next lambda or
+                            // XSPH pass filters (written by permute_step, delta_apply, fill_quads)
   const SegParams *segs;
   int nseg;
   int n;                    // total particles
@@ -244,12 +264,18 @@ void launch_key_only(const DeviceState &d, const float4 *pred, cudaStream_t st);
 void launch_scan(const DeviceState &d, cudaStream_t st);
 void launch_scatter(const DeviceState &d, cudaStream_t st);
 void launch_cell_sort(const DeviceState &d, cudaStream_t st);
+// writes pred_out and its copy in d.quads
 void launch_permute_step(const DeviceState &d, float4 *pred_out, const float4 *normal_in, cudaStream_t st);
 void launch_permute_all(const DeviceState &d, const float4 *pred_in, float4 *pred_out, cudaStream_t st);
 // neighbour passes
 void launch_normal(const DeviceState &d, const float4 *pred, float4 *out, cudaStream_t st);
 void launch_lambda(const DeviceState &d, const float4 *pred, cudaStream_t st);
-// fused substep (exact = the reference's expressions, else re-associated)
+// d.quads <- pred (the per-pass API's lambda, whose input was not written
+// by permute_step or delta_apply)
+void launch_fill_quads(const DeviceState &d, const float4 *pred, cudaStream_t st);
+// fused substep (exact = the reference's expressions, else re-associated).
+// lambda and xsph_finalize filter candidates from d.quads, which must hold
+// `pred`: permute_step and delta_apply leave there what they write.
 void launch_lambda_f(const DeviceState &d, const float4 *pred, bool exact, cudaStream_t st);
 void launch_delta_apply_f(const DeviceState &d, const float4 *pred_in, float4 *pred_out, bool exact, cudaStream_t st);
 // record / recorded: the XSPH pass leaves its row masks for the next

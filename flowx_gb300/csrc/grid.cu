@@ -307,6 +307,7 @@ __global__ void k_permute_step(DeviceState d, float4 *__restrict__ pred_out, con
   if (sp.sigma > 0.0f) d.normal[k] = n;
   d.pos_alt[k] = p;
   pred_out[k] = make_float4(q.x, q.y, q.z, 1.0f);
+  store_quad(d.quads, k, q.x, q.y, q.z);
   d.ids[k] = (uint32_t)(pr >> 32);
   d.keys[k] = d.key_tmp[s];
 }

@@ -141,6 +141,71 @@ __device__ __forceinline__ bool build_row_masks(const SegParams &s, const uint32
   return true;
 }
 
+// pair_r2 of two candidates at once, from q - p: negating a difference is
+// exact and squares drop the sign, so each lane equals pair_r2<EXACT>(p - q)
+// bit for bit (EXACT: (dx*dx + dy*dy) + dz*dz, each operation rounded;
+// FAST: the same fused multiply-adds as pair_r2).
+template <bool EXACT>
+__device__ __forceinline__ float2 pair_r2_x2(float2 qx, float2 qy, float2 qz, float2 npx, float2 npy, float2 npz)
+{
+  const float2 dx = __fadd2_rn(qx, npx), dy = __fadd2_rn(qy, npy), dz = __fadd2_rn(qz, npz);
+  if (EXACT) return __fadd2_rn(__fadd2_rn(__fmul2_rn(dx, dx), __fmul2_rn(dy, dy)), __fmul2_rn(dz, dz));
+  return __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+}
+
+// build_row_masks over the slot quads: the same masks, four candidates per
+// three 16-byte loads. A row [ra, rb) is covered by the quads ra/4 .. (rb-1)/4;
+// quad t's accept bits go to bits 4t..4t+3 of a 68-bit word (ex:hi:lo), whose
+// ra % 4 lowest bits (slots before ra) are then shifted out and whose bits
+// from rb - ra on (slots past the row) are cleared.
+template <bool EXACT>
+__device__ __forceinline__ bool build_row_masks_quads(const SegParams &s, const uint32_t *__restrict__ off,
+                                                      const SlotQuad *__restrict__ quads, float4 p, float lim2,
+                                                      int3 base, unsigned long long *mine, int stride)
+{
+  const int x0 = max(base.x - 1, 0), x1 = min(base.x + 1, s.nx - 1);
+  const float2 npx = make_float2(-p.x, -p.x), npy = make_float2(-p.y, -p.y), npz = make_float2(-p.z, -p.z);
+#pragma unroll 1
+  for (int r = 0; r < kRows; ++r) {
+    const int z = base.z + (r / 3) - 1;
+    const int y = base.y + (r % 3) - 1;
+    unsigned long long mm = 0ull;
+    if (z >= 0 && z < s.nz && y >= 0 && y < s.ny) {
+      const int row = s.c_begin + (z * s.ny + y) * s.nx;
+      const uint32_t ra = __ldg(&off[row + x0]);
+      const uint32_t rb = __ldg(&off[row + x1 + 1]);
+      const uint32_t len = rb - ra;
+      if (len > 64u) return false;
+      if (len != 0u) {
+        uint32_t lo = 0u, hi = 0u, ex = 0u;
+        const uint32_t g1 = (rb + 3u) >> 2;
+#pragma unroll 1
+        for (uint32_t g = ra >> 2, sh = 0u; g < g1; ++g, sh += 4u) {
+          const float4 X = __ldg(&quads[g].x), Y = __ldg(&quads[g].y), Z = __ldg(&quads[g].z);
+          const float2 a = pair_r2_x2<EXACT>(make_float2(X.x, X.y), make_float2(Y.x, Y.y), make_float2(Z.x, Z.y),
+                                             npx, npy, npz);
+          const float2 b = pair_r2_x2<EXACT>(make_float2(X.z, X.w), make_float2(Y.z, Y.w), make_float2(Z.z, Z.w),
+                                             npx, npy, npz);
+          const uint32_t nib = (a.x < lim2 ? 1u : 0u) | (a.y < lim2 ? 2u : 0u) | (b.x < lim2 ? 4u : 0u) |
+                               (b.y < lim2 ? 8u : 0u);
+          if (sh < 32u)
+            lo |= nib << sh;
+          else if (sh < 64u)
+            hi |= nib << (sh - 32u);
+          else
+            ex = nib;
+        }
+        mm = ((unsigned long long)hi << 32) | lo;
+        const uint32_t lead = ra & 3u;
+        if (lead != 0u) mm = (mm >> lead) | ((unsigned long long)ex << (64u - lead));
+        if (len < 64u) mm &= (1ull << len) - 1ull;
+      }
+    }
+    mine[r * stride] = mm;
+  }
+  return true;
+}
+
 // Phase 2: every set bit of every row, rows in order, slots ascending; each
 // lane moves to its next row when its current mask runs out. GUARDED (masks
 // recorded by an earlier launch): rows outside the grid and bits past a row's
@@ -209,16 +274,33 @@ struct MaskRecord {
   int n;
 };
 
-// for_each_within that also records slot i's masks.
+// for_each_within with phase 1 over the slot quads (quads[k / 4] lane k % 4
+// holding pos[k]).
+template <bool EXACT, class F>
+__device__ __forceinline__ void for_each_within(const SegParams &s, const uint32_t *__restrict__ off,
+                                                const float4 *__restrict__ pos, const SlotQuad *__restrict__ quads,
+                                                float4 p, float lim2, int3 base, F &&f)
+{
+  extern __shared__ unsigned long long row_masks[];
+  unsigned long long *mine = row_masks + threadIdx.x;
+  if (build_row_masks_quads<EXACT>(s, off, quads, p, lim2, base, mine, blockDim.x))
+    visit_row_masks<false>(s, off, base, mine, blockDim.x, f);
+  else
+    for_each_within_rows<EXACT>(s, off, pos, p, lim2, base, f);
+}
+
+// for_each_within (phase 1 over the slot quads) that also records slot i's
+// masks.
 template <bool EXACT, class F>
 __device__ __forceinline__ void for_each_within_recording(const SegParams &s, const uint32_t *__restrict__ off,
-                                                          const float4 *__restrict__ pos, float4 p, float lim2,
+                                                          const float4 *__restrict__ pos,
+                                                          const SlotQuad *__restrict__ quads, float4 p, float lim2,
                                                           int3 base, MaskRecord rec, int i, F &&f)
 {
   extern __shared__ unsigned long long row_masks[];
   unsigned long long *mine = row_masks + threadIdx.x;
   const int stride = blockDim.x;
-  const bool ok = build_row_masks<EXACT>(s, off, pos, p, lim2, base, mine, stride);
+  const bool ok = build_row_masks_quads<EXACT>(s, off, quads, p, lim2, base, mine, stride);
   rec.wide[i] = ok ? 0 : 1;
   if (ok) {
 #pragma unroll

@@ -48,7 +48,7 @@ __global__ void __launch_bounds__(512, 3) k_lambda_f(DeviceState d, const float4
   const int3 base = cell_coord(s, pi.x, pi.y, pi.z);
   LambdaAcc<EXACT> acc;
   const MaskRecord rec{d.row_masks, d.row_wide, d.n};
-  for_each_within_recording<EXACT>(s, d.offsets, pred, pi, s.h2, base, rec, i, [&](int k) {
+  for_each_within_recording<EXACT>(s, d.offsets, pred, d.quads, pi, s.h2, base, rec, i, [&](int k) {
     const float4 pj = __ldg(&pred[k]);
     acc.pair(s, pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, k == i);
   });
@@ -92,14 +92,25 @@ __global__ void __launch_bounds__(512) k_delta_apply_f(DeviceState d, const floa
   const float4 pi = pred_in[i];
   const float3 a = delta_sum_f<EXACT, true>(s, d, pred_in, i, pi);
   const float rest = s.rest;
-  pred_out[i] = make_float4(pi.x + a.x / rest, pi.y + a.y / rest, pi.z + a.z / rest, 1.0f);
+  const float4 q = make_float4(pi.x + a.x / rest, pi.y + a.y / rest, pi.z + a.z / rest, 1.0f);
+  pred_out[i] = q;
+  store_quad(d.quads, i, q.x, q.y, q.z);
+}
+
+__global__ void k_fill_quads(DeviceState d, const float4 *__restrict__ pred)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.n) return;
+  const float4 q = pred[i];
+  store_quad(d.quads, i, q.x, q.y, q.z);
 }
 
 // sph_xsph.glsl:35-81: c * sum (m / rho_j) (v_j - v_i) W(r), neighbour
 // velocities from velj(k, pred_k).
 // record: leave the row masks for the next substep's normal pass, which
-// tests the same positions against this grid with the same reach.
-template <bool EXACT, class VelJ>
+// tests the same positions against this grid with the same reach. QUADS:
+// d.quads holds pred (the fused substep), so phase 1 reads the quads.
+template <bool EXACT, bool QUADS, class VelJ>
 __device__ __forceinline__ float3 xsph_sum_f(const SegParams &s, const DeviceState &d, const float4 *__restrict__ pred,
                                              int i, float4 q, float3 vi, bool record, VelJ &&velj)
 {
@@ -128,9 +139,11 @@ __device__ __forceinline__ float3 xsph_sum_f(const SegParams &s, const DeviceSta
       az = __fmaf_rn(wk, __fsub_rn(vj.z, vi.z), az);
     }
   };
-  if (record)
-    for_each_within_recording<EXACT>(s, d.offsets, pred, q, h2, base, MaskRecord{d.row_masks, d.row_wide, d.n}, i,
-                                     body);
+  if (QUADS && record)
+    for_each_within_recording<EXACT>(s, d.offsets, pred, d.quads, q, h2, base,
+                                     MaskRecord{d.row_masks, d.row_wide, d.n}, i, body);
+  else if (QUADS)
+    for_each_within<EXACT>(s, d.offsets, pred, d.quads, q, h2, base, body);
   else
     for_each_within<EXACT>(s, d.offsets, pred, q, h2, base, body);
   const float c = s.visc;
@@ -156,7 +169,7 @@ __global__ void __launch_bounds__(512, 3) k_xsph_finalize_f(DeviceState d, const
     vi = make_float3(__fmul_rn(__fsub_rn(q.x, p0.x), inv_dtc), __fmul_rn(__fsub_rn(q.y, p0.y), inv_dtc),
                      __fmul_rn(__fsub_rn(q.z, p0.z), inv_dtc));
   }
-  const float3 dv = xsph_sum_f<EXACT>(s, d, pred, i, q, vi, record != 0, [&](int k, const float4 &pj) {
+  const float3 dv = xsph_sum_f<EXACT, true>(s, d, pred, i, q, vi, record != 0, [&](int k, const float4 &pj) {
     const float4 pk = __ldg(&pos_in[k]);
     if (EXACT) return slot_velocity(pj, pk, dtc);
     return make_float3(__fmul_rn(__fsub_rn(pj.x, pk.x), inv_dtc), __fmul_rn(__fsub_rn(pj.y, pk.y), inv_dtc),
@@ -293,7 +306,7 @@ __global__ void __launch_bounds__(512) k_xsph(DeviceState d, const float4 *__res
   FLOWX_SLOT_PROLOGUE
   const float4 vi4 = d.vel[i];
   const float4 *__restrict__ vel = d.vel;
-  const float3 dv = xsph_sum_f<true>(s, d, pred, i, pred[i], make_float3(vi4.x, vi4.y, vi4.z), false,
+  const float3 dv = xsph_sum_f<true, false>(s, d, pred, i, pred[i], make_float3(vi4.x, vi4.y, vi4.z), false,
                                      [&](int k, const float4 &) {
                                        const float4 v = __ldg(&vel[k]);
                                        return make_float3(v.x, v.y, v.z);
@@ -316,7 +329,15 @@ void launch_normal(const DeviceState &d, const float4 *pred, float4 *out, cudaSt
 {
   launch_normal_f(d, pred, out, true, false, st);
 }
-void launch_lambda(const DeviceState &d, const float4 *pred, cudaStream_t st) { launch_lambda_f(d, pred, true, st); }
+void launch_fill_quads(const DeviceState &d, const float4 *pred, cudaStream_t st)
+{
+  if (d.n > 0) k_fill_quads<<<grid_for(d.n, 256), 256, 0, st>>>(d, pred);
+}
+void launch_lambda(const DeviceState &d, const float4 *pred, cudaStream_t st)
+{
+  launch_fill_quads(d, pred, st);
+  launch_lambda_f(d, pred, true, st);
+}
 void launch_predict(const DeviceState &d, float4 *pred, cudaStream_t st)
 {
   if (d.n > 0) k_predict<<<grid_for(d.n, 256), 256, 0, st>>>(d, pred);

@@ -158,6 +158,7 @@ int Ctx::allocate()
   FLOWX_ALLOC(d_segs, (size_t)std::max<int>((int)segs.size(), 1))
   FLOWX_ALLOC(d_src_slot, n)
   FLOWX_ALLOC(d.row_masks, n * 9) FLOWX_ALLOC(d.row_wide, n) FLOWX_ALLOC(d.cell_lo, c) FLOWX_ALLOC(d.cell_hi, c)
+  FLOWX_ALLOC(d.quads, (n + 3) / 4)
 #undef FLOWX_ALLOC
   if (e != cudaSuccess) return cuda(e, "device allocation");
   d.segs = d_segs;
@@ -180,7 +181,7 @@ void Ctx::release()
   void *ptrs[] = {d.pos,    d.pos_alt, d.vel,       d.vel_alt,  d.pred_a,   d.pred_b,  d.normal,     d.normal_alt,
                   d.delta,  d.delta_alt, d.lam,     d.lam_alt,  d.stage,    d.keys,    d.ids,        d.key_tmp,
                   d.rank_tmp, d.pairs, d.pairs_tmp, d.counts,   d.offsets,  d.block_sums, d.big_cells, d.collider,
-                  d.surface, d_segs,   d_src_slot,  d_prims,  d.row_masks, d.row_wide, d.cell_lo, d.cell_hi};
+                  d.surface, d_segs,   d_src_slot,  d_prims,  d.row_masks, d.row_wide, d.cell_lo, d.cell_hi, d.quads};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (stream) cudaStreamDestroy(stream);
