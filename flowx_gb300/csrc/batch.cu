@@ -64,7 +64,7 @@ int snapshot(Ctx *c, Snapshot &s, bool save)
     s.normal_in_order = c->normal_in_order;
     s.delta_in_order = c->delta_in_order;
   } else {
-    c->xsph_masks_valid = false;  // recorded masks describe the state being replaced
+    c->next_normals_valid = false;  // the pending normals describe the state being replaced
     c->pred_idx = s.pred_idx;
     c->normal_zero = s.normal_zero;
     c->normal_in_order = s.normal_in_order;
@@ -289,7 +289,7 @@ int flowx_autotune(flowx_ctx *ctx, const flowx_push *push, int iterations, int32
   }
   if (rc == FLOWX_OK) rc = c->cuda(cudaStreamSynchronize(c->stream), "autotune");
   release(snap);
-  c->xsph_masks_valid = false;  // the restored state is not the one the last trial's masks describe
+  c->next_normals_valid = false;  // the restored state is not the one the last trial's normals describe
   if (rc) {
     std::memcpy(c->d.block, before, sizeof(before));
     return rc;

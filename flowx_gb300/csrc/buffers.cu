@@ -77,7 +77,7 @@ int Ctx::ensure_offsets()
 // Move every per-particle array so that new slot k holds old slot src_slot[k].
 int Ctx::reorder_state(const std::vector<uint32_t> &src_slot)
 {
-  xsph_masks_valid = false;
+  next_normals_valid = false;
   const int n = total_particles;
   if (n == 0) return FLOWX_OK;
   int rc = cuda(cudaMemcpyAsync(d_src_slot, src_slot.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, stream),
@@ -147,7 +147,7 @@ int flowx_upload(flowx_ctx *ctx, int buffer, const void *host, size_t bytes)
   if (!ctx) return FLOWX_ERR_ARG;
   Ctx *c = reinterpret_cast<Ctx *>(ctx);
   cudaSetDevice(c->device);
-  c->xsph_masks_valid = false;
+  c->next_normals_valid = false;
   const int n = c->total_particles;
   if (!host && bytes) return c->fail(FLOWX_ERR_ARG, "host pointer is NULL");
   if (particle_f4_buffer(buffer) || buffer == FLOWX_BUF_LAMBDA) {
@@ -447,9 +447,8 @@ int Ctx::profile_substeps(int iterations, int substeps, float *ms, int32_t *laun
   for (int s = 0; s < substeps; ++s) {
     float4 *pin = c->pred_cur();
     const bool sigma = c->segs_need_normal();
-    const bool recorded = c->xsph_masks_valid;
-    if (sigma)
-      timed(K_NORMAL, 1, [&] { launch_normal_f(d, pin, d.normal_alt, exact, recorded, c->stream); });
+    if (sigma && !c->next_normals_valid)
+      timed(K_NORMAL, 1, [&] { launch_normal_f(d, pin, d.normal_alt, exact, c->stream); });
     timed(K_PREDICT_KEY, 1, [&] { launch_predict_key(d, d.normal_alt, c->stream); });
     timed(K_SCAN_REDUCE, 3, [&] { launch_scan(d, c->stream); });
     timed(K_SCATTER, 1, [&] { launch_scatter(d, c->stream); });

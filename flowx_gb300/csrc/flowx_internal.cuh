@@ -278,13 +278,13 @@ void launch_fill_quads(const DeviceState &d, const float4 *pred, cudaStream_t st
 // `pred`: permute_step and delta_apply leave there what they write.
 void launch_lambda_f(const DeviceState &d, const float4 *pred, bool exact, cudaStream_t st);
 void launch_delta_apply_f(const DeviceState &d, const float4 *pred_in, float4 *pred_out, bool exact, cudaStream_t st);
-// record / recorded: the XSPH pass leaves its row masks for the next
-// substep's normal pass (same positions, same grid, same reach), which may
-// then skip its candidate tests; the caller vouches that nothing changed
-// positions, grid or slot order in between.
+// normals: the XSPH pass also evaluates the next substep's normal pass (same
+// positions, densities and grid) into d.normal_alt; the next substep then
+// skips its normal pass, the caller vouching that nothing changed positions,
+// densities, parameters, grid or slot order in between.
 void launch_xsph_finalize_f(const DeviceState &d, const float4 *pred, const float4 *pos_in, float4 *pos_out,
-                            bool keep_delta, bool exact, bool record, cudaStream_t st);
-void launch_normal_f(const DeviceState &d, const float4 *pred, float4 *out, bool exact, bool recorded, cudaStream_t st);
+                            bool keep_delta, bool exact, bool normals, cudaStream_t st);
+void launch_normal_f(const DeviceState &d, const float4 *pred, float4 *out, bool exact, cudaStream_t st);
 // The splat of one segment (cells [cell_begin, cell_begin + cell_count)):
 // refreshes those cells' position bounds, then gathers every sample.
 void launch_splat_segment(const DeviceState &d, int seg, int cell_begin, int cell_count, const float *surface_lo,

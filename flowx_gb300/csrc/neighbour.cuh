@@ -207,11 +207,8 @@ __device__ __forceinline__ bool build_row_masks_quads(const SegParams &s, const 
 }
 
 // Phase 2: every set bit of every row, rows in order, slots ascending; each
-// lane moves to its next row when its current mask runs out. GUARDED (masks
-// recorded by an earlier launch): rows outside the grid and bits past a row's
-// current length are dropped, so a mask can never name a slot outside its
-// row, whatever happened in between.
-template <bool GUARDED, class F>
+// lane moves to its next row when its current mask runs out.
+template <class F>
 __device__ __forceinline__ void visit_row_masks(const SegParams &s, const uint32_t *__restrict__ off, int3 base,
                                                 const unsigned long long *mine, int stride, F &&f)
 {
@@ -229,18 +226,7 @@ __device__ __forceinline__ void visit_row_masks(const SegParams &s, const uint32
       const int z = base.z + (r / 3) - 1;
       const int y = base.y + (r % 3) - 1;
       const int row = s.c_begin + (z * s.ny + y) * s.nx;
-      if (GUARDED) {
-        if (z < 0 || z >= s.nz || y < 0 || y >= s.ny) {
-          m = 0ull;
-          continue;
-        }
-        ra = __ldg(&off[row + x0]);
-        const uint32_t len = __ldg(&off[row + x1 + 1]) - ra;
-        if (len < 64u) m &= (1ull << len) - 1ull;
-        if (m == 0ull) continue;
-      } else {
-        ra = __ldg(&off[row + x0]);
-      }
+      ra = __ldg(&off[row + x0]);
     }
     const int t = __ffsll((long long)m) - 1;
     m &= m - 1ull;
@@ -259,7 +245,7 @@ __device__ __forceinline__ void for_each_within(const SegParams &s, const uint32
   extern __shared__ unsigned long long row_masks[];
   unsigned long long *mine = row_masks + threadIdx.x;
   if (build_row_masks<EXACT>(s, off, pos, p, lim2, base, mine, blockDim.x))
-    visit_row_masks<false>(s, off, base, mine, blockDim.x, f);
+    visit_row_masks(s, off, base, mine, blockDim.x, f);
   else
     for_each_within_rows<EXACT>(s, off, pos, p, lim2, base, f);
 }
@@ -284,7 +270,7 @@ __device__ __forceinline__ void for_each_within(const SegParams &s, const uint32
   extern __shared__ unsigned long long row_masks[];
   unsigned long long *mine = row_masks + threadIdx.x;
   if (build_row_masks_quads<EXACT>(s, off, quads, p, lim2, base, mine, blockDim.x))
-    visit_row_masks<false>(s, off, base, mine, blockDim.x, f);
+    visit_row_masks(s, off, base, mine, blockDim.x, f);
   else
     for_each_within_rows<EXACT>(s, off, pos, p, lim2, base, f);
 }
@@ -305,16 +291,15 @@ __device__ __forceinline__ void for_each_within_recording(const SegParams &s, co
   if (ok) {
 #pragma unroll
     for (int r = 0; r < kRows; ++r) rec.masks[(size_t)r * rec.n + i] = mine[r * stride];
-    visit_row_masks<false>(s, off, base, mine, stride, f);
+    visit_row_masks(s, off, base, mine, stride, f);
   } else {
     for_each_within_rows<EXACT>(s, off, pos, p, lim2, base, f);
   }
 }
 
-// for_each_within from slot i's recorded masks (same positions, grid and
-// reach as the recording pass): phase 2 only. GUARDED when the masks were
-// recorded by a launch of an earlier call (see visit_row_masks).
-template <bool EXACT, bool GUARDED, class F>
+// for_each_within from slot i's recorded masks, left by the launch just
+// before on the same stream (same positions, grid and reach): phase 2 only.
+template <bool EXACT, class F>
 __device__ __forceinline__ void for_each_within_recorded(const SegParams &s, const uint32_t *__restrict__ off,
                                                          const float4 *__restrict__ pos, float4 p, float lim2,
                                                          int3 base, MaskRecord rec, int i, F &&f)
@@ -328,7 +313,7 @@ __device__ __forceinline__ void for_each_within_recorded(const SegParams &s, con
   }
 #pragma unroll
   for (int r = 0; r < kRows; ++r) mine[r * stride] = __ldg(&rec.masks[(size_t)r * rec.n + i]);
-  visit_row_masks<GUARDED>(s, off, base, mine, stride, f);
+  visit_row_masks(s, off, base, mine, stride, f);
 }
 
 // ---- pass bodies ----------------------------------------------------------

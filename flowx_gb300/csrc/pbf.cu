@@ -76,8 +76,8 @@ __device__ __forceinline__ float3 delta_sum_f(const SegParams &s, const DeviceSt
     delta_pair<EXACT>(s, lambda_i, __ldg(&d.lam[k].y), dx, dy, dz, r2, ax, ay, az);
   };
   if (RECORDED)
-    for_each_within_recorded<EXACT, false>(s, d.offsets, pred, pi, h2, base, MaskRecord{d.row_masks, d.row_wide, d.n},
-                                           i, body);
+    for_each_within_recorded<EXACT>(s, d.offsets, pred, pi, h2, base, MaskRecord{d.row_masks, d.row_wide, d.n},
+                                    i, body);
   else
     for_each_within<EXACT>(s, d.offsets, pred, pi, h2, base, body);
   return make_float3(ax, ay, az);
@@ -106,17 +106,21 @@ __global__ void k_fill_quads(DeviceState d, const float4 *__restrict__ pred)
 }
 
 // sph_xsph.glsl:35-81: c * sum (m / rho_j) (v_j - v_i) W(r), neighbour
-// velocities from velj(k, pred_k).
-// record: leave the row masks for the next substep's normal pass, which
-// tests the same positions against this grid with the same reach. QUADS:
-// d.quads holds pred (the fused substep), so phase 1 reads the quads.
-template <bool EXACT, bool QUADS, class VelJ>
+// velocities from velj(k, pred_k). QUADS: d.quads holds pred (the fused
+// substep), so phase 1 reads the quads. NORMALS (slots whose segment has
+// sigma > 0): the same walk also evaluates sph_normal.glsl:24-81 for these
+// positions, densities and grid - exactly the inputs the next substep's
+// normal pass reads, since nothing between this pass and that one changes
+// them - and leaves the result in *normal_out.
+template <bool EXACT, bool QUADS, bool NORMALS, class VelJ>
 __device__ __forceinline__ float3 xsph_sum_f(const SegParams &s, const DeviceState &d, const float4 *__restrict__ pred,
-                                             int i, float4 q, float3 vi, bool record, VelJ &&velj)
+                                             int i, float4 q, float3 vi, VelJ &&velj, float4 *normal_out = nullptr)
 {
   const int3 base = cell_coord(s, q.x, q.y, q.z);
-  const float h2 = s.h2, mass = s.mass, poly6 = s.poly6;
+  const float h = s.h, h2 = s.h2, mass = s.mass, poly6 = s.poly6;
+  const bool normals = NORMALS && s.sigma > 0.0f;
   float ax = 0.0f, ay = 0.0f, az = 0.0f;
+  float nx = 0.0f, ny = 0.0f, nz = 0.0f, lap = 0.0f;
   auto body = [&](int k) {
     if (k == i) return;
     const float4 pj = __ldg(&pred[k]);
@@ -131,31 +135,51 @@ __device__ __forceinline__ float3 xsph_sum_f(const SegParams &s, const DeviceSta
       ax += (w * (vj.x - vi.x)) * wk;
       ay += (w * (vj.y - vi.y)) * wk;
       az += (w * (vj.z - vi.z)) * wk;
+      if (normals) {  // sph_normal.glsl's body, as k_normal_f
+        const float t = h2 - r2;
+        const float sg = s.poly6m6 * t * t;
+        nx += w * (sg * dx);
+        ny += w * (sg * dy);
+        nz += w * (sg * dz);
+        lap += w * w_visc_lap(sqrtf(r2), h, s.visclap);
+      }
     } else {
       const float t = __fsub_rn(h2, r2);
       const float wk = __fmul_rn(__fdividef(s.mass_poly6, rho_j), __fmul_rn(__fmul_rn(t, t), t));
       ax = __fmaf_rn(wk, __fsub_rn(vj.x, vi.x), ax);
       ay = __fmaf_rn(wk, __fsub_rn(vj.y, vi.y), ay);
       az = __fmaf_rn(wk, __fsub_rn(vj.z, vi.z), az);
+      if (normals) {
+        const float weight = __fdividef(mass, rho_j);
+        const float sg = __fmul_rn(weight, __fmul_rn(s.poly6m6, __fmul_rn(t, t)));
+        nx = __fmaf_rn(sg, dx, nx);
+        ny = __fmaf_rn(sg, dy, ny);
+        nz = __fmaf_rn(sg, dz, nz);
+        const float r = r2 > 0.0f ? __fmul_rn(r2, rsqrtf(r2)) : 0.0f;
+        lap = __fmaf_rn(__fmul_rn(weight, s.visclap), __fsub_rn(h, r), lap);
+      }
     }
   };
-  if (QUADS && record)
-    for_each_within_recording<EXACT>(s, d.offsets, pred, d.quads, q, h2, base,
-                                     MaskRecord{d.row_masks, d.row_wide, d.n}, i, body);
-  else if (QUADS)
+  if (QUADS)
     for_each_within<EXACT>(s, d.offsets, pred, d.quads, q, h2, base, body);
   else
     for_each_within<EXACT>(s, d.offsets, pred, q, h2, base, body);
+  if (normals) {
+    const float mag = sqrtf(nx * nx + ny * ny + nz * nz);
+    const float curv = (mag > 1e-4f) ? -lap / mag : 0.0f;
+    *normal_out = make_float4(nx, ny, nz, curv);
+  }
   const float c = s.visc;
   return make_float3(c * ax, c * ay, c * az);
 }
 
 // sph_velocity.glsl + sph_xsph.glsl + sph_finalize.glsl.
-template <bool EXACT>
+// NORMALS: also the next substep's normals, into d.normal_alt (the slot order
+// of this grid, which the next substep's permute maps to its own).
+template <bool EXACT, bool NORMALS>
 __global__ void __launch_bounds__(512, 3) k_xsph_finalize_f(DeviceState d, const float4 *__restrict__ pred,
                                                          const float4 *__restrict__ pos_in,
-                                                         float4 *__restrict__ pos_out, int keep_delta,
-                                                         int record)
+                                                         float4 *__restrict__ pos_out, int keep_delta)
 {
   FLOWX_SLOT_PROLOGUE
   const float dtc = s.dtc;
@@ -169,12 +193,15 @@ __global__ void __launch_bounds__(512, 3) k_xsph_finalize_f(DeviceState d, const
     vi = make_float3(__fmul_rn(__fsub_rn(q.x, p0.x), inv_dtc), __fmul_rn(__fsub_rn(q.y, p0.y), inv_dtc),
                      __fmul_rn(__fsub_rn(q.z, p0.z), inv_dtc));
   }
-  const float3 dv = xsph_sum_f<EXACT, true>(s, d, pred, i, q, vi, record != 0, [&](int k, const float4 &pj) {
-    const float4 pk = __ldg(&pos_in[k]);
-    if (EXACT) return slot_velocity(pj, pk, dtc);
-    return make_float3(__fmul_rn(__fsub_rn(pj.x, pk.x), inv_dtc), __fmul_rn(__fsub_rn(pj.y, pk.y), inv_dtc),
-                       __fmul_rn(__fsub_rn(pj.z, pk.z), inv_dtc));
-  });
+  const float3 dv = xsph_sum_f<EXACT, true, NORMALS>(
+      s, d, pred, i, q, vi,
+      [&](int k, const float4 &pj) {
+        const float4 pk = __ldg(&pos_in[k]);
+        if (EXACT) return slot_velocity(pj, pk, dtc);
+        return make_float3(__fmul_rn(__fsub_rn(pj.x, pk.x), inv_dtc), __fmul_rn(__fsub_rn(pj.y, pk.y), inv_dtc),
+                           __fmul_rn(__fsub_rn(pj.z, pk.z), inv_dtc));
+      },
+      d.normal_alt + i);
   float3 v = make_float3(vi.x + dv.x, vi.y + dv.y, vi.z + dv.z);
   float3 p = make_float3(q.x, q.y, q.z);
   finalize_particle(s, d.collider, p, v);
@@ -183,12 +210,12 @@ __global__ void __launch_bounds__(512, 3) k_xsph_finalize_f(DeviceState d, const
   if (keep_delta) d.delta[i] = make_float4(dv.x, dv.y, dv.z, 0.0f);
 }
 
-// sph_normal.glsl:24-81 (over the previous substep's grid, as the reference).
-// recorded: the previous substep's XSPH pass left its row masks for these
-// positions, this grid and this reach.
+// sph_normal.glsl:24-81 (over the previous substep's grid, as the reference);
+// the fused substep runs it only when the previous substep's XSPH pass did
+// not already evaluate it (the first substep, or state changed in between).
 template <bool EXACT>
 __global__ void __launch_bounds__(512, 3) k_normal_f(DeviceState d, const float4 *__restrict__ pred,
-                                                  float4 *__restrict__ out, int recorded)
+                                                  float4 *__restrict__ out)
 {
   FLOWX_SLOT_PROLOGUE
   const float4 pi = pred[i];
@@ -223,11 +250,7 @@ __global__ void __launch_bounds__(512, 3) k_normal_f(DeviceState d, const float4
       lap = __fmaf_rn(__fmul_rn(weight, vlap), __fsub_rn(h, r), lap);
     }
   };
-  if (recorded)
-    for_each_within_recorded<EXACT, true>(s, d.offsets, pred, pi, h2, base, MaskRecord{d.row_masks, d.row_wide, d.n},
-                                          i, body);
-  else
-    for_each_within<EXACT>(s, d.offsets, pred, pi, h2, base, body);
+  for_each_within<EXACT>(s, d.offsets, pred, pi, h2, base, body);
   const float mag = sqrtf(nx * nx + ny * ny + nz * nz);
   const float curv = (mag > 1e-4f) ? -lap / mag : 0.0f;
   out[i] = make_float4(nx, ny, nz, curv);
@@ -249,21 +272,27 @@ void launch_delta_apply_f(const DeviceState &d, const float4 *pred_in, float4 *p
   else k_delta_apply_f<false><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred_in, pred_out);
 }
 void launch_xsph_finalize_f(const DeviceState &d, const float4 *pred, const float4 *pos_in, float4 *pos_out,
-                            bool keep_delta, bool exact, bool record, cudaStream_t st)
+                            bool keep_delta, bool exact, bool normals, cudaStream_t st)
 {
-  const int b = FLOWX_BLOCK(d, K_XSPH_FINALIZE, 128,
-                            exact ? (const void *)k_xsph_finalize_f<true> : (const void *)k_xsph_finalize_f<false>);
+  const void *fn = exact ? (normals ? (const void *)k_xsph_finalize_f<true, true>
+                                    : (const void *)k_xsph_finalize_f<true, false>)
+                         : (normals ? (const void *)k_xsph_finalize_f<false, true>
+                                    : (const void *)k_xsph_finalize_f<false, false>);
+  const int b = FLOWX_BLOCK(d, K_XSPH_FINALIZE, 128, fn);
   if (d.n <= 0) return;
   const size_t sm = row_mask_bytes(b);
-  if (exact) k_xsph_finalize_f<true><<<grid_for(d.n, b), b, sm, st>>>(d, pred, pos_in, pos_out, keep_delta, record);
-  else k_xsph_finalize_f<false><<<grid_for(d.n, b), b, sm, st>>>(d, pred, pos_in, pos_out, keep_delta, record);
+  const unsigned g = grid_for(d.n, b);
+  if (exact && normals) k_xsph_finalize_f<true, true><<<g, b, sm, st>>>(d, pred, pos_in, pos_out, keep_delta);
+  else if (exact) k_xsph_finalize_f<true, false><<<g, b, sm, st>>>(d, pred, pos_in, pos_out, keep_delta);
+  else if (normals) k_xsph_finalize_f<false, true><<<g, b, sm, st>>>(d, pred, pos_in, pos_out, keep_delta);
+  else k_xsph_finalize_f<false, false><<<g, b, sm, st>>>(d, pred, pos_in, pos_out, keep_delta);
 }
-void launch_normal_f(const DeviceState &d, const float4 *pred, float4 *out, bool exact, bool recorded, cudaStream_t st)
+void launch_normal_f(const DeviceState &d, const float4 *pred, float4 *out, bool exact, cudaStream_t st)
 {
   const int b = FLOWX_BLOCK(d, K_NORMAL, 128, exact ? (const void *)k_normal_f<true> : (const void *)k_normal_f<false>);
   if (d.n <= 0) return;
-  if (exact) k_normal_f<true><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred, out, recorded);
-  else k_normal_f<false><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred, out, recorded);
+  if (exact) k_normal_f<true><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred, out);
+  else k_normal_f<false><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred, out);
 }
 
 // ---- single reference passes (per-pass API; always exact) ------------------
@@ -306,11 +335,11 @@ __global__ void __launch_bounds__(512) k_xsph(DeviceState d, const float4 *__res
   FLOWX_SLOT_PROLOGUE
   const float4 vi4 = d.vel[i];
   const float4 *__restrict__ vel = d.vel;
-  const float3 dv = xsph_sum_f<true, false>(s, d, pred, i, pred[i], make_float3(vi4.x, vi4.y, vi4.z), false,
-                                     [&](int k, const float4 &) {
-                                       const float4 v = __ldg(&vel[k]);
-                                       return make_float3(v.x, v.y, v.z);
-                                     });
+  const float3 dv = xsph_sum_f<true, false, false>(s, d, pred, i, pred[i], make_float3(vi4.x, vi4.y, vi4.z),
+                                                  [&](int k, const float4 &) {
+                                                    const float4 v = __ldg(&vel[k]);
+                                                    return make_float3(v.x, v.y, v.z);
+                                                  });
   d.delta[i] = make_float4(dv.x, dv.y, dv.z, 0.0f);
 }
 // sph_finalize.glsl:15-96
@@ -327,7 +356,7 @@ __global__ void k_finalize(DeviceState d, const float4 *__restrict__ pred)
 
 void launch_normal(const DeviceState &d, const float4 *pred, float4 *out, cudaStream_t st)
 {
-  launch_normal_f(d, pred, out, true, false, st);
+  launch_normal_f(d, pred, out, true, st);
 }
 void launch_fill_quads(const DeviceState &d, const float4 *pred, cudaStream_t st)
 {

@@ -231,7 +231,7 @@ int Ctx::set_push(const flowx_push *push)
 int Ctx::upload_segs(const std::vector<SegParams> &s, int cells)
 {
   const bool same = s.size() == segs.size() && std::memcmp(s.data(), segs.data(), s.size() * sizeof(SegParams)) == 0;
-  if (!same || cells != d.cells) xsph_masks_valid = false;  // reach or geometry changed
+  if (!same || cells != d.cells) next_normals_valid = false;  // reach or geometry changed
   if (!same || !segs_uploaded) {
     if (s.size() > seg_capacity) {
       // A batch with more scenes than the table holds: grow it (stream work
@@ -273,7 +273,7 @@ void Ctx::issue_build_from_pred(const float4 *pred)
 
 int Ctx::build_grid_generic()
 {
-  xsph_masks_valid = false;
+  next_normals_valid = false;
   float4 *src = pred_cur();
   float4 *dst = pred_idx == 0 ? d.pred_b : d.pred_a;
   issue_build_from_pred(src);
@@ -299,17 +299,17 @@ int Ctx::build_grid_generic()
 
 // The fused substep body (see pbf.cu's header for the pass mapping).
 // pred_in_idx: predicted buffer holding last substep's corrected predictions.
-int Ctx::issue_substep(int iterations, int pred_in_idx, bool normal_recorded)
+int Ctx::issue_substep(int iterations, int pred_in_idx, bool normals_ready)
 {
   float4 *pred_in = pred_in_idx == 0 ? d.pred_a : d.pred_b;
   const bool sigma = segs_need_normal();
   const bool exact = (flags & FLOWX_FLAG_EXACT) != 0;
   // The substep's normals go to scratch in the old slot order; the permute
   // moves them to the new order in the canonical buffer. The normal pass
-  // walks the previous substep's grid, with the row masks that substep's XSPH
-  // pass recorded when normal_recorded.
-  if (sigma) {
-    launch_normal_f(d, pred_in, d.normal_alt, exact, normal_recorded, stream);
+  // walks the previous substep's grid; when normals_ready, that substep's
+  // XSPH pass already evaluated it there.
+  if (sigma && !normals_ready) {
+    launch_normal_f(d, pred_in, d.normal_alt, exact, stream);
     g_launches += 1;
   }
   launch_predict_key(d, d.normal_alt, stream);
@@ -336,7 +336,7 @@ int Ctx::issue_substep(int iterations, int pred_in_idx, bool normal_recorded)
 // FLOWX_FLAG_KEEP_DELTA. The others can no longer be mapped to particle ids.
 void Ctx::after_fused_substep()
 {
-  xsph_masks_valid = segs_need_normal();
+  next_normals_valid = segs_need_normal();
   if (segs_need_normal()) {
     normal_zero = false;
   } else if (!normal_zero) {
@@ -365,7 +365,7 @@ int Ctx::substep(int iterations)
 {
   int rc = ensure_grid();
   if (rc) return rc;
-  issue_substep(iterations, pred_idx, xsph_masks_valid);
+  issue_substep(iterations, pred_idx, next_normals_valid);
   pred_idx = iterations % 2 == 0 ? 0 : 1;
   keys_host_valid = false;
   after_fused_substep();
@@ -377,7 +377,7 @@ int Ctx::step(int iterations, int substeps)
   int rc = ensure_grid();
   if (rc) return rc;
   const int end_idx = iterations % 2 == 0 ? 0 : 1;
-  GraphKey key{iterations, substeps, pred_idx, d.cells, segs_need_normal() ? 1 : 0, flags, xsph_masks_valid ? 1 : 0};
+  GraphKey key{iterations, substeps, pred_idx, d.cells, segs_need_normal() ? 1 : 0, flags, next_normals_valid ? 1 : 0};
   auto it = graphs.find(key);
   if (it == graphs.end()) {
     cudaGraph_t graph = nullptr;
@@ -386,7 +386,7 @@ int Ctx::step(int iterations, int substeps)
     const long long before = g_launches.load();
     int idx = pred_idx;
     for (int s = 0; s < substeps; ++s) {
-      issue_substep(iterations, idx, s > 0 || xsph_masks_valid);
+      issue_substep(iterations, idx, s > 0 || next_normals_valid);
       idx = end_idx;
     }
     const long long kernels = g_launches.load() - before;
@@ -536,7 +536,7 @@ int flowx_run_pass(flowx_ctx *ctx, int pass_id, const flowx_push *push)
                           pass_id == FLOWX_PASS_DELTA || pass_id == FLOWX_PASS_XSPH;
   if (needs_grid && !c->have_grid)
     return c->fail(FLOWX_ERR_STATE, "neighbour pass before any grid build: call flowx_build_grid first");
-  c->xsph_masks_valid = false;
+  c->next_normals_valid = false;
   switch (pass_id) {
     case FLOWX_PASS_NORMAL:
       launch_normal(d, pred, d.normal, c->stream);

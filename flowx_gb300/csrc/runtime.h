@@ -51,8 +51,9 @@ struct Ctx {
   bool normal_zero = true;         // normal holds only the zeros it was created with
   bool normal_in_order = true;     // normal / delta still follow the slot order
   bool delta_in_order = true;
-  bool xsph_masks_valid = false;   // the last fused substep's XSPH row masks still describe
-                                   // pred_cur() against the current grid and reach
+  bool next_normals_valid = false;  // normal_alt holds the normal pass of pred_cur() against the
+                                    // current grid and parameters (left by the last fused
+                                    // substep's XSPH pass)
   int collider_dims[3] = {0, 0, 0};
   std::string err;
   std::map<GraphKey, GraphEntry> graphs;
