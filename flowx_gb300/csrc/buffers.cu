@@ -457,11 +457,13 @@ int Ctx::profile_substeps(int iterations, int substeps, float *ms, int32_t *laun
     float4 *q_in = d.pred_a, *q_out = d.pred_b;
     for (int it = 0; it < iterations; ++it) {
       timed(K_LAMBDA, 1, [&] { launch_lambda_f(d, q_in, exact, c->stream); });
-      timed(K_DELTA_APPLY, 1, [&] { launch_delta_apply_f(d, q_in, q_out, exact, c->stream); });
+      const bool last = it == iterations - 1;
+      timed(K_DELTA_APPLY, 1, [&] { launch_delta_apply_f(d, q_in, q_out, exact, last, c->stream); });
       std::swap(q_in, q_out);
     }
+    if (iterations == 0) launch_xsph_inputs(d, q_in, exact, c->stream);
     timed(K_XSPH_FINALIZE, 1, [&] {
-      launch_xsph_finalize_f(d, q_in, d.pos_alt, d.pos, (c->flags & FLOWX_FLAG_KEEP_DELTA) != 0, exact, sigma,
+      launch_xsph_finalize_f(d, q_in, d.pos, (c->flags & FLOWX_FLAG_KEEP_DELTA) != 0, exact, sigma,
                              c->stream);
     });
     c->pred_idx = end_idx;

@@ -148,6 +148,8 @@ struct DeviceState {
   float4 *cell_lo, *cell_hi;  // per cell: bounds of its particles' positions (the splat's cell test)
   unsigned long long *row_masks;  // the lambda pass's neighbour masks, 9 per slot (row-major)
   uint8_t *row_wide;        // per slot: masks not recorded (a row over 64 slots)
+  float4 *plam;             // per slot: predicted position and lambda of the last lambda pass
+  float4 *xv;               // per slot: velocity (pred - pos) / dt and max(rho, 1e-6) entering XSPH
   SlotQuad *quads;          // ceil(n / 4) groups: the predicted positions the next lambda or
                             // XSPH pass filters (written by permute_step, delta_apply, fill_quads)
   const SegParams *segs;
@@ -277,13 +279,18 @@ void launch_fill_quads(const DeviceState &d, const float4 *pred, cudaStream_t st
 // lambda and xsph_finalize filter candidates from d.quads, which must hold
 // `pred`: permute_step and delta_apply leave there what they write.
 void launch_lambda_f(const DeviceState &d, const float4 *pred, bool exact, cudaStream_t st);
-void launch_delta_apply_f(const DeviceState &d, const float4 *pred_in, float4 *pred_out, bool exact, cudaStream_t st);
+// last: the substep's final iteration, which also leaves d.xv for XSPH
+void launch_delta_apply_f(const DeviceState &d, const float4 *pred_in, float4 *pred_out, bool exact, bool last,
+                          cudaStream_t st);
+// d.xv from pred and the substep's starting positions, for a substep with no
+// Jacobi iteration
+void launch_xsph_inputs(const DeviceState &d, const float4 *pred, bool exact, cudaStream_t st);
 // normals: the XSPH pass also evaluates the next substep's normal pass (same
 // positions, densities and grid) into d.normal_alt; the next substep then
 // skips its normal pass, the caller vouching that nothing changed positions,
 // densities, parameters, grid or slot order in between.
-void launch_xsph_finalize_f(const DeviceState &d, const float4 *pred, const float4 *pos_in, float4 *pos_out,
-                            bool keep_delta, bool exact, bool normals, cudaStream_t st);
+void launch_xsph_finalize_f(const DeviceState &d, const float4 *pred, float4 *pos_out, bool keep_delta, bool exact,
+                            bool normals, cudaStream_t st);
 void launch_normal_f(const DeviceState &d, const float4 *pred, float4 *out, bool exact, cudaStream_t st);
 // The splat of one segment (cells [cell_begin, cell_begin + cell_count)):
 // refreshes those cells' position bounds, then gathers every sample.

@@ -52,13 +52,17 @@ __global__ void __launch_bounds__(512, 3) k_lambda_f(DeviceState d, const float4
     const float4 pj = __ldg(&pred[k]);
     acc.pair(s, pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, k == i);
   });
-  d.lam[i] = acc.finish(s);
+  const float2 l = acc.finish(s);
+  d.lam[i] = l;
+  d.plam[i] = make_float4(pi.x, pi.y, pi.z, l.y);
 }
 
 // sph_delta.glsl:19-85, summed correction before the 1/rho0 scale. RECORDED:
 // the lambda pass of this iteration just tested the same positions against
 // the same grid with the same reach (r < h), so its recorded row masks stand
 // in for phase 1; the body keeps its own j != i and r^2 > 1e-12 tests.
+// RECORDED also reads each neighbour's position and lambda from d.plam (one
+// 16-byte load; the lambda pass left them there).
 template <bool EXACT, bool RECORDED>
 __device__ __forceinline__ float3 delta_sum_f(const SegParams &s, const DeviceState &d, const float4 *__restrict__ pred,
                                               int i, float4 pi)
@@ -69,11 +73,11 @@ __device__ __forceinline__ float3 delta_sum_f(const SegParams &s, const DeviceSt
   const float h2 = s.h2;
   auto body = [&](int k) {
     if (k == i) return;
-    const float4 pj = __ldg(&pred[k]);
+    const float4 pj = RECORDED ? __ldg(&d.plam[k]) : __ldg(&pred[k]);
     const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
     const float r2 = pair_r2<EXACT>(dx, dy, dz);
     if (r2 >= h2 || r2 <= 1e-12f) return;
-    delta_pair<EXACT>(s, lambda_i, __ldg(&d.lam[k].y), dx, dy, dz, r2, ax, ay, az);
+    delta_pair<EXACT>(s, lambda_i, RECORDED ? pj.w : __ldg(&d.lam[k].y), dx, dy, dz, r2, ax, ay, az);
   };
   if (RECORDED)
     for_each_within_recorded<EXACT>(s, d.offsets, pred, pi, h2, base, MaskRecord{d.row_masks, d.row_wide, d.n},
@@ -83,10 +87,31 @@ __device__ __forceinline__ float3 delta_sum_f(const SegParams &s, const DeviceSt
   return make_float3(ax, ay, az);
 }
 
+// What the XSPH pass needs of slot i besides its position: the velocity
+// sph_velocity.glsl:20-23 derives from pred and the substep's starting
+// position (the same expression XSPH evaluated per neighbour), and the
+// density floor sph_xsph.glsl applies.
+template <bool EXACT>
+__device__ __forceinline__ float4 xsph_input(const SegParams &s, const DeviceState &d, int i, float4 q)
+{
+  const float4 p0 = d.pos_alt[i];
+  const float dtc = s.dtc;
+  float3 v;
+  if (EXACT) {
+    v = slot_velocity(q, p0, dtc);
+  } else {
+    const float inv_dtc = 1.0f / dtc;
+    v = make_float3(__fmul_rn(__fsub_rn(q.x, p0.x), inv_dtc), __fmul_rn(__fsub_rn(q.y, p0.y), inv_dtc),
+                    __fmul_rn(__fsub_rn(q.z, p0.z), inv_dtc));
+  }
+  return make_float4(v.x, v.y, v.z, fmaxf(d.lam[i].x, 1e-6f));
+}
+
 // sph_delta.glsl + sph_apply_delta.glsl: pred_out = pred_in + sum / rho0.
+// last: also d.xv[i] for the XSPH pass that follows.
 template <bool EXACT>
 __global__ void __launch_bounds__(512) k_delta_apply_f(DeviceState d, const float4 *__restrict__ pred_in,
-                                                       float4 *__restrict__ pred_out)
+                                                       float4 *__restrict__ pred_out, int last)
 {
   FLOWX_SLOT_PROLOGUE
   const float4 pi = pred_in[i];
@@ -95,6 +120,14 @@ __global__ void __launch_bounds__(512) k_delta_apply_f(DeviceState d, const floa
   const float4 q = make_float4(pi.x + a.x / rest, pi.y + a.y / rest, pi.z + a.z / rest, 1.0f);
   pred_out[i] = q;
   store_quad(d.quads, i, q.x, q.y, q.z);
+  if (last) d.xv[i] = xsph_input<EXACT>(s, d, i, q);
+}
+
+template <bool EXACT>
+__global__ void k_xsph_inputs(DeviceState d, const float4 *__restrict__ pred)
+{
+  FLOWX_SLOT_PROLOGUE
+  d.xv[i] = xsph_input<EXACT>(s, d, i, pred[i]);
 }
 
 __global__ void k_fill_quads(DeviceState d, const float4 *__restrict__ pred)
@@ -112,6 +145,8 @@ __global__ void k_fill_quads(DeviceState d, const float4 *__restrict__ pred)
 // positions, densities and grid - exactly the inputs the next substep's
 // normal pass reads, since nothing between this pass and that one changes
 // them - and leaves the result in *normal_out.
+// The fused pass (QUADS) takes each neighbour's velocity and density from
+// d.xv, left by the last delta_apply.
 template <bool EXACT, bool QUADS, bool NORMALS, class VelJ>
 __device__ __forceinline__ float3 xsph_sum_f(const SegParams &s, const DeviceState &d, const float4 *__restrict__ pred,
                                              int i, float4 q, float3 vi, VelJ &&velj, float4 *normal_out = nullptr)
@@ -127,8 +162,16 @@ __device__ __forceinline__ float3 xsph_sum_f(const SegParams &s, const DeviceSta
     const float dx = q.x - pj.x, dy = q.y - pj.y, dz = q.z - pj.z;
     const float r2 = pair_r2<EXACT>(dx, dy, dz);
     if (r2 >= h2) return;
-    const float rho_j = fmaxf(__ldg(&d.lam[k].x), 1e-6f);
-    const float3 vj = velj(k, pj);
+    float rho_j;
+    float3 vj;
+    if (QUADS) {
+      const float4 xj = __ldg(&d.xv[k]);
+      rho_j = xj.w;
+      vj = make_float3(xj.x, xj.y, xj.z);
+    } else {
+      rho_j = fmaxf(__ldg(&d.lam[k].x), 1e-6f);
+      vj = velj(k, pj);
+    }
     if (EXACT) {
       const float w = mass / rho_j;
       const float wk = w_poly6(r2, h2, poly6);
@@ -178,30 +221,14 @@ __device__ __forceinline__ float3 xsph_sum_f(const SegParams &s, const DeviceSta
 // of this grid, which the next substep's permute maps to its own).
 template <bool EXACT, bool NORMALS>
 __global__ void __launch_bounds__(512, 3) k_xsph_finalize_f(DeviceState d, const float4 *__restrict__ pred,
-                                                         const float4 *__restrict__ pos_in,
                                                          float4 *__restrict__ pos_out, int keep_delta)
 {
   FLOWX_SLOT_PROLOGUE
-  const float dtc = s.dtc;
-  const float inv_dtc = 1.0f / dtc;
   const float4 q = pred[i];
-  const float4 p0 = pos_in[i];
-  float3 vi;
-  if (EXACT) {
-    vi = slot_velocity(q, p0, dtc);
-  } else {
-    vi = make_float3(__fmul_rn(__fsub_rn(q.x, p0.x), inv_dtc), __fmul_rn(__fsub_rn(q.y, p0.y), inv_dtc),
-                     __fmul_rn(__fsub_rn(q.z, p0.z), inv_dtc));
-  }
+  const float4 xi = d.xv[i];
+  const float3 vi = make_float3(xi.x, xi.y, xi.z);
   const float3 dv = xsph_sum_f<EXACT, true, NORMALS>(
-      s, d, pred, i, q, vi,
-      [&](int k, const float4 &pj) {
-        const float4 pk = __ldg(&pos_in[k]);
-        if (EXACT) return slot_velocity(pj, pk, dtc);
-        return make_float3(__fmul_rn(__fsub_rn(pj.x, pk.x), inv_dtc), __fmul_rn(__fsub_rn(pj.y, pk.y), inv_dtc),
-                           __fmul_rn(__fsub_rn(pj.z, pk.z), inv_dtc));
-      },
-      d.normal_alt + i);
+      s, d, pred, i, q, vi, [](int, const float4 &) { return make_float3(0.f, 0.f, 0.f); }, d.normal_alt + i);
   float3 v = make_float3(vi.x + dv.x, vi.y + dv.y, vi.z + dv.z);
   float3 p = make_float3(q.x, q.y, q.z);
   finalize_particle(s, d.collider, p, v);
@@ -263,16 +290,24 @@ void launch_lambda_f(const DeviceState &d, const float4 *pred, bool exact, cudaS
   if (exact) k_lambda_f<true><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred);
   else k_lambda_f<false><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred);
 }
-void launch_delta_apply_f(const DeviceState &d, const float4 *pred_in, float4 *pred_out, bool exact, cudaStream_t st)
+void launch_delta_apply_f(const DeviceState &d, const float4 *pred_in, float4 *pred_out, bool exact, bool last,
+                          cudaStream_t st)
 {
   const int b = FLOWX_BLOCK(d, K_DELTA_APPLY, 128,
                             exact ? (const void *)k_delta_apply_f<true> : (const void *)k_delta_apply_f<false>);
   if (d.n <= 0) return;
-  if (exact) k_delta_apply_f<true><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred_in, pred_out);
-  else k_delta_apply_f<false><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred_in, pred_out);
+  const int l = last ? 1 : 0;
+  if (exact) k_delta_apply_f<true><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred_in, pred_out, l);
+  else k_delta_apply_f<false><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred_in, pred_out, l);
 }
-void launch_xsph_finalize_f(const DeviceState &d, const float4 *pred, const float4 *pos_in, float4 *pos_out,
-                            bool keep_delta, bool exact, bool normals, cudaStream_t st)
+void launch_xsph_inputs(const DeviceState &d, const float4 *pred, bool exact, cudaStream_t st)
+{
+  if (d.n <= 0) return;
+  if (exact) k_xsph_inputs<true><<<grid_for(d.n, 256), 256, 0, st>>>(d, pred);
+  else k_xsph_inputs<false><<<grid_for(d.n, 256), 256, 0, st>>>(d, pred);
+}
+void launch_xsph_finalize_f(const DeviceState &d, const float4 *pred, float4 *pos_out, bool keep_delta, bool exact,
+                            bool normals, cudaStream_t st)
 {
   const void *fn = exact ? (normals ? (const void *)k_xsph_finalize_f<true, true>
                                     : (const void *)k_xsph_finalize_f<true, false>)
@@ -282,10 +317,10 @@ void launch_xsph_finalize_f(const DeviceState &d, const float4 *pred, const floa
   if (d.n <= 0) return;
   const size_t sm = row_mask_bytes(b);
   const unsigned g = grid_for(d.n, b);
-  if (exact && normals) k_xsph_finalize_f<true, true><<<g, b, sm, st>>>(d, pred, pos_in, pos_out, keep_delta);
-  else if (exact) k_xsph_finalize_f<true, false><<<g, b, sm, st>>>(d, pred, pos_in, pos_out, keep_delta);
-  else if (normals) k_xsph_finalize_f<false, true><<<g, b, sm, st>>>(d, pred, pos_in, pos_out, keep_delta);
-  else k_xsph_finalize_f<false, false><<<g, b, sm, st>>>(d, pred, pos_in, pos_out, keep_delta);
+  if (exact && normals) k_xsph_finalize_f<true, true><<<g, b, sm, st>>>(d, pred, pos_out, keep_delta);
+  else if (exact) k_xsph_finalize_f<true, false><<<g, b, sm, st>>>(d, pred, pos_out, keep_delta);
+  else if (normals) k_xsph_finalize_f<false, true><<<g, b, sm, st>>>(d, pred, pos_out, keep_delta);
+  else k_xsph_finalize_f<false, false><<<g, b, sm, st>>>(d, pred, pos_out, keep_delta);
 }
 void launch_normal_f(const DeviceState &d, const float4 *pred, float4 *out, bool exact, cudaStream_t st)
 {

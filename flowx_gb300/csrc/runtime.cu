@@ -158,7 +158,7 @@ int Ctx::allocate()
   FLOWX_ALLOC(d_segs, (size_t)std::max<int>((int)segs.size(), 1))
   FLOWX_ALLOC(d_src_slot, n)
   FLOWX_ALLOC(d.row_masks, n * 9) FLOWX_ALLOC(d.row_wide, n) FLOWX_ALLOC(d.cell_lo, c) FLOWX_ALLOC(d.cell_hi, c)
-  FLOWX_ALLOC(d.quads, (n + 3) / 4)
+  FLOWX_ALLOC(d.quads, (n + 3) / 4) FLOWX_ALLOC(d.plam, n) FLOWX_ALLOC(d.xv, n)
 #undef FLOWX_ALLOC
   if (e != cudaSuccess) return cuda(e, "device allocation");
   d.segs = d_segs;
@@ -181,7 +181,7 @@ void Ctx::release()
   void *ptrs[] = {d.pos,    d.pos_alt, d.vel,       d.vel_alt,  d.pred_a,   d.pred_b,  d.normal,     d.normal_alt,
                   d.delta,  d.delta_alt, d.lam,     d.lam_alt,  d.stage,    d.keys,    d.ids,        d.key_tmp,
                   d.rank_tmp, d.pairs, d.pairs_tmp, d.counts,   d.offsets,  d.block_sums, d.big_cells, d.collider,
-                  d.surface, d_segs,   d_src_slot,  d_prims,  d.row_masks, d.row_wide, d.cell_lo, d.cell_hi, d.quads};
+                  d.surface, d_segs,   d_src_slot,  d_prims,  d.row_masks, d.row_wide, d.cell_lo, d.cell_hi, d.quads, d.plam, d.xv};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (stream) cudaStreamDestroy(stream);
@@ -321,11 +321,15 @@ int Ctx::issue_substep(int iterations, int pred_in_idx, bool normals_ready)
   float4 *q_in = d.pred_a, *q_out = d.pred_b;
   for (int it = 0; it < iterations; ++it) {
     launch_lambda_f(d, q_in, exact, stream);
-    launch_delta_apply_f(d, q_in, q_out, exact, stream);
+    launch_delta_apply_f(d, q_in, q_out, exact, it == iterations - 1, stream);
     g_launches += 2;
     std::swap(q_in, q_out);
   }
-  launch_xsph_finalize_f(d, q_in, d.pos_alt, d.pos, (flags & FLOWX_FLAG_KEEP_DELTA) != 0, exact, sigma, stream);
+  if (iterations == 0) {
+    launch_xsph_inputs(d, q_in, exact, stream);
+    g_launches += 1;
+  }
+  launch_xsph_finalize_f(d, q_in, d.pos, (flags & FLOWX_FLAG_KEEP_DELTA) != 0, exact, sigma, stream);
   g_launches += 1;
   return FLOWX_OK;
 }
