@@ -630,7 +630,7 @@ def run_flowx(args):
     adjoint = None
     if rank == 0 and not args.no_adjoint:
         adjoint = _adjoint_metrics()
-    other_configs = _other_configs() if rank == 0 else None
+    other_configs = _other_configs() if rank == 0 and not args.no_other_configs else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -704,6 +704,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-scene batched measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-substep measurement")
+    ap.add_argument("--no-other-configs", action="store_true",
+                    help="skip the dam-break and pool measurements (profiler launch lists of the workload alone)")
     ap.add_argument("--case", action="store_true",
                     help="untimed launch-by-launch run of --warmup frames, for profiler captures")
     ap.add_argument("--exact", action="store_true", help="with --case: the reference's float expressions")
