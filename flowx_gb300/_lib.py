@@ -91,6 +91,16 @@ class Primitive(ctypes.Structure):
     ]
 
 
+class Mesh(ctypes.Structure):
+    _fields_ = [
+        ("vertices", ctypes.POINTER(ctypes.c_float)),
+        ("vertex_count", ctypes.c_int32),
+        ("triangles", ctypes.POINTER(ctypes.c_int32)),
+        ("triangle_count", ctypes.c_int32),
+        ("matrix_world", ctypes.c_float * 16),
+    ]
+
+
 class AdjointConfig(ctypes.Structure):
     """flowx_adjoint_config (include/flowx.h)."""
 
@@ -154,6 +164,9 @@ def load(path: str | None = None):
         "flowx_set_collider": ([ctx, vp, P(ctypes.c_int32), ctypes.c_float], ctypes.c_int),
         "flowx_voxelize": ([ctx, P(Primitive), ctypes.c_int, P(ctypes.c_int32), ctypes.c_float, P(ctypes.c_float)],
                            ctypes.c_int),
+        "flowx_voxelize_meshes": ([ctx, P(Mesh), ctypes.c_int, P(ctypes.c_int32), ctypes.c_float, P(ctypes.c_float)],
+                                  ctypes.c_int),
+        "flowx_download_collider": ([ctx, vp, ctypes.c_size_t], ctypes.c_int),
         "flowx_build_grid": ([ctx, P(Push)], ctypes.c_int),
         "flowx_substep": ([ctx, P(Push), ctypes.c_int], ctypes.c_int),
         "flowx_step": ([ctx, P(Push), ctypes.c_int, ctypes.c_int], ctypes.c_int),

@@ -181,7 +181,7 @@ void Ctx::release()
   void *ptrs[] = {d.pos,    d.pos_alt, d.vel,       d.vel_alt,  d.pred_a,   d.pred_b,  d.normal,     d.normal_alt,
                   d.delta,  d.delta_alt, d.lam,     d.lam_alt,  d.stage,    d.keys,    d.ids,        d.key_tmp,
                   d.rank_tmp, d.pairs, d.pairs_tmp, d.counts,   d.offsets,  d.block_sums, d.big_cells, d.collider,
-                  d.surface, d_segs,   d_src_slot,  d_prims,  d.row_masks, d.row_wide, d.cell_lo, d.cell_hi, d.quads, d.plam, d.xv};
+                  d.surface, d_segs,   d_src_slot,  d_prims,  d_mesh,  d.row_masks, d.row_wide, d.cell_lo, d.cell_hi, d.quads, d.plam, d.xv};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (stream) cudaStreamDestroy(stream);

@@ -17,7 +17,7 @@ float bits_to_float(int32_t b);
 void seg_from_push(const flowx_push &p, SegParams &s);
 
 // (iterations, substeps, starting predicted buffer, cells, normal pass on, flags,
-// first normal pass reuses the previous XSPH masks)
+// first substep's normal pass already evaluated by the previous XSPH pass)
 using GraphKey = std::tuple<int, int, int, int, int, int, int>;
 struct GraphEntry {
   cudaGraphExec_t exec = nullptr;
@@ -39,6 +39,8 @@ struct Ctx {
   uint32_t *d_src_slot = nullptr;  // reorder scratch for key uploads
   void *d_prims = nullptr;         // voxeliser primitives
   int prim_cap = 0;
+  void *d_mesh = nullptr;          // mesh voxeliser scratch (vertices, triangles, world vertices, flips)
+  size_t mesh_cap = 0;
   std::vector<SegParams> segs;
   bool segs_uploaded = false;
   size_t seg_capacity = 1;         // entries the device segment table holds
@@ -70,7 +72,7 @@ struct Ctx {
   int upload_segs(const std::vector<SegParams> &s, int cells);
   void issue_build_from_pred(const float4 *pred);
   int build_grid_generic();
-  int issue_substep(int iterations, int pred_in_idx, bool normal_recorded);
+  int issue_substep(int iterations, int pred_in_idx, bool normals_ready);
   bool segs_need_normal() const;
   void after_fused_substep();
   int ensure_grid();

@@ -183,6 +183,35 @@ class Solver:
         self.collider_dims = tuple(int(v) for v in dims)
         self.collider_voxel = float(voxel)
 
+    def voxelize_meshes(self, meshes, dims, voxel: float, origin=None):
+        """Build the collider grid on the GPU from triangle meshes
+        (collision/__init__.py:304-367 and the union of :225-242): each mesh a
+        (vertices V x 3, triangles T x 3, matrix_world 4 x 4) triple in the
+        object's local space and Blender's row-major world matrix."""
+        keep = []
+        arr = (_lib.Mesh * max(len(meshes), 1))()
+        for i, (verts, tris, matrix) in enumerate(meshes):
+            v = np.ascontiguousarray(verts, np.float32).reshape(-1, 3)
+            t = np.ascontiguousarray(tris, np.int32).reshape(-1, 3)
+            keep += [v, t]
+            arr[i].vertices = v.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+            arr[i].vertex_count = v.shape[0]
+            arr[i].triangles = t.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+            arr[i].triangle_count = t.shape[0]
+            arr[i].matrix_world[:] = tuple(float(x) for x in np.asarray(matrix, np.float32).reshape(16))
+        d = (ctypes.c_int32 * 3)(*dims)
+        o = (ctypes.c_float * 3)(*(origin if origin is not None else self.config.lo))
+        check(self.lib.flowx_voxelize_meshes(self._ctx, arr, len(meshes), d, float(voxel), o), self._ctx)
+        self.collider_dims = tuple(int(v) for v in dims)
+        self.collider_voxel = float(voxel)
+
+    def collider_occupancy(self) -> np.ndarray:
+        """The installed collider grid, (nz, ny, nx) uint8 (1 = occupied)."""
+        nx, ny, nz = self.collider_dims
+        out = np.empty((nz, ny, nx), np.uint8)
+        check(self.lib.flowx_download_collider(self._ctx, out.ctypes.data, out.nbytes), self._ctx)
+        return out
+
     def clear_collider(self):
         check(self.lib.flowx_set_collider(self._ctx, None, None, 0.0), self._ctx)
         self.collider_dims = None

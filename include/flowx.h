@@ -174,6 +174,37 @@ int flowx_set_collider(flowx_ctx *ctx, const uint8_t *occupancy, const int32_t d
 int flowx_voxelize(flowx_ctx *ctx, const flowx_primitive *prims, int count, const int32_t dims[3],
                    float voxel_size, const float origin[3]);
 
+/* One triangle-mesh collider for flowx_voxelize_meshes(): local-space
+ * vertices (vertex_count x 3 floats), triangles (triangle_count x 3 vertex
+ * indices) and the object's world matrix (4 x 4, row-major, applied to column
+ * vectors: world = M [v; 1], Blender's matrix_world). */
+typedef struct flowx_mesh {
+  const float *vertices;
+  int32_t vertex_count;
+  const int32_t *triangles;
+  int32_t triangle_count;
+  float matrix_world[16];
+} flowx_mesh;
+
+/* Build the collider grid on the device from triangle meshes: a voxel is
+ * occupied when its centre is inside any mesh, by the parity of the mesh's
+ * crossings of the vertical ray above the centre, each mesh marking only the
+ * voxels of its world bounding box's index range; a mesh with a singular
+ * matrix marks nothing. Replaces collision/__init__.py:304-367
+ * (_rebuild_grid, _point_inside: BVH ray casts on the CPU) and the union of
+ * :225-242; crossings are counted exactly in double precision with
+ * watertight edge tests rather than by Blender's ray casts. Same layout as
+ * flowx_set_collider; triangle indices outside [0, vertex_count) are
+ * rejected before anything runs. */
+int flowx_voxelize_meshes(flowx_ctx *ctx, const flowx_mesh *meshes, int count, const int32_t dims[3],
+                          float voxel_size, const float origin[3]);
+
+/* Read back the installed collider grid (the flowx_set_collider layout, one
+ * byte per voxel, 1 = occupied): the occupancy collision/__init__.py keeps on
+ * the CPU for its viewport overlay (ColliderGrid.occupancy). bytes must equal
+ * the installed grid's voxel count; waits for the copy. */
+int flowx_download_collider(flowx_ctx *ctx, uint8_t *host, size_t bytes);
+
 /* The neighbour grid from the current predicted positions: keys, cell ranges
  * and the particle order. Replaces solver/sph.py:482-498 (_build_grid: the
  * grid-key pass, the bitonic (k, j) dispatch loop, cell clear, cell range). */
