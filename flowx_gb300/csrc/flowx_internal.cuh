@@ -153,21 +153,20 @@ struct DeviceState {
   SlotQuad *quads;          // ceil(n / 4) groups: the predicted positions the next lambda or
                             // XSPH pass filters (written by permute_step, delta_apply, fill_quads)
   const SegParams *segs;
+  int32_t *slot_seg;        // per slot: its segment (read only when nseg > 1)
   int nseg;
   int n;                    // total particles
   int cells;                // total cells
   int sm_count;             // multiprocessors of the context's device
 };
 
-// Segment of slot k (segments are sorted by p_begin).
-__device__ __forceinline__ int seg_of_slot(const SegParams *__restrict__ segs, int nseg, int k)
+// Segment of slot k. A segment's particles keep its slot range
+// [p_begin, p_begin + p_count) through every grid build (its cells are a
+// contiguous range holding exactly its particles), so the table is written
+// once per segment-table upload.
+__device__ __forceinline__ int slot_segment(const DeviceState &d, int k)
 {
-  int lo = 0, hi = nseg - 1;
-  while (lo < hi) {
-    int mid = (lo + hi + 1) >> 1;
-    if (__ldg(&segs[mid].p_begin) <= k) lo = mid; else hi = mid - 1;
-  }
-  return lo;
+  return d.nseg == 1 ? 0 : __ldg(&d.slot_seg[k]);
 }
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }

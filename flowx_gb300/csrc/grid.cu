@@ -48,7 +48,7 @@ __global__ void k_predict_key(DeviceState d, const float4 *__restrict__ normal_i
   const bool active = k < d.n;
   uint32_t key = 0;
   if (active) {
-    const SegParams &s = d.segs[seg_of_slot(d.segs, d.nseg, k)];
+    const SegParams &s = d.segs[slot_segment(d, k)];
     const float4 p = d.pos[k];
     const float4 v = d.vel[k];
     const float4 n = s.sigma > 0.0f ? normal_in[k] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -70,7 +70,7 @@ __global__ void k_key_only(DeviceState d, const float4 *__restrict__ pred)
   const bool active = k < d.n;
   uint32_t key = 0;
   if (active) {
-    const SegParams &s = d.segs[seg_of_slot(d.segs, d.nseg, k)];
+    const SegParams &s = d.segs[slot_segment(d, k)];
     const float4 q = pred[k];
     key = (uint32_t)(s.c_begin + cell_index(s, cell_coord(s, q.x, q.y, q.z)));
     d.key_tmp[k] = key;
@@ -298,7 +298,7 @@ __global__ void k_permute_step(DeviceState d, float4 *__restrict__ pred_out, con
   if (k >= d.n) return;
   const unsigned long long pr = d.pairs[k];
   const int s = (int)(uint32_t)pr;
-  const SegParams &sp = d.segs[seg_of_slot(d.segs, d.nseg, k)];
+  const SegParams &sp = d.segs[slot_segment(d, k)];
   const float4 p = d.pos[s];
   const float4 v = d.vel[s];
   const float4 n = sp.sigma > 0.0f ? normal_in[s] : make_float4(0.f, 0.f, 0.f, 0.f);

@@ -25,7 +25,7 @@ static inline unsigned grid_for(long long n, int b) { return (unsigned)((n + b -
 #define FLOWX_SLOT_PROLOGUE                            \
   const int i = blockIdx.x * blockDim.x + threadIdx.x; \
   if (i >= d.n) return;                                \
-  const SegParams &s = d.segs[seg_of_slot(d.segs, d.nseg, i)];
+  const SegParams &s = d.segs[slot_segment(d, i)];
 
 // sph_velocity.glsl:20-23 for one slot.
 __device__ __forceinline__ float3 slot_velocity(const float4 &q, const float4 &p, float dtc)

@@ -158,7 +158,7 @@ int Ctx::allocate()
   FLOWX_ALLOC(d_segs, (size_t)std::max<int>((int)segs.size(), 1))
   FLOWX_ALLOC(d_src_slot, n)
   FLOWX_ALLOC(d.row_masks, n * 9) FLOWX_ALLOC(d.row_wide, n) FLOWX_ALLOC(d.cell_lo, c) FLOWX_ALLOC(d.cell_hi, c)
-  FLOWX_ALLOC(d.quads, (n + 3) / 4) FLOWX_ALLOC(d.plam, n) FLOWX_ALLOC(d.xv, n)
+  FLOWX_ALLOC(d.quads, (n + 3) / 4) FLOWX_ALLOC(d.plam, n) FLOWX_ALLOC(d.xv, n) FLOWX_ALLOC(d.slot_seg, n)
 #undef FLOWX_ALLOC
   if (e != cudaSuccess) return cuda(e, "device allocation");
   d.segs = d_segs;
@@ -181,7 +181,7 @@ void Ctx::release()
   void *ptrs[] = {d.pos,    d.pos_alt, d.vel,       d.vel_alt,  d.pred_a,   d.pred_b,  d.normal,     d.normal_alt,
                   d.delta,  d.delta_alt, d.lam,     d.lam_alt,  d.stage,    d.keys,    d.ids,        d.key_tmp,
                   d.rank_tmp, d.pairs, d.pairs_tmp, d.counts,   d.offsets,  d.block_sums, d.big_cells, d.collider,
-                  d.surface, d_segs,   d_src_slot,  d_prims,  d_mesh,  d.row_masks, d.row_wide, d.cell_lo, d.cell_hi, d.quads, d.plam, d.xv};
+                  d.surface, d_segs,   d_src_slot,  d_prims,  d_mesh,  d.row_masks, d.row_wide, d.cell_lo, d.cell_hi, d.quads, d.plam, d.xv, d.slot_seg};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (stream) cudaStreamDestroy(stream);
@@ -250,6 +250,19 @@ int Ctx::upload_segs(const std::vector<SegParams> &s, int cells)
                                   stream),
                   "segment table upload");
     if (rc) return rc;
+    if (segs.size() > 1) {
+      // slot -> segment (the pageable copy is staged before this returns)
+      std::vector<int32_t> owner((size_t)total_particles, 0);
+      for (size_t k = 0; k < segs.size(); ++k)
+        for (int q = 0; q < segs[k].p_count; ++q) {
+          const long long slot = (long long)segs[k].p_begin + q;
+          if (slot >= 0 && slot < total_particles) owner[(size_t)slot] = (int32_t)k;
+        }
+      rc = cuda(cudaMemcpyAsync(d.slot_seg, owner.data(), owner.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                stream),
+                "slot segment table upload");
+      if (rc) return rc;
+    }
     segs_uploaded = true;
     d.segs = d_segs;
     d.nseg = (int)segs.size();
