@@ -43,9 +43,11 @@ __device__ __forceinline__ float pair_r2(float dx, float dy, float dz)
 
 // Visit the candidates k of the 3x3x3 stencil around `base` whose position
 // pos[k] satisfies pair_r2<EXACT>(p - pos[k]) < lim2, in the reference's
-// order; `f(k)` is called for each. Rows whose run exceeds 64 slots are
-// walked directly with the reference's per-cell MAX_CELL_SCAN cap, calling
-// f for every candidate of the row (the body repeats its own test).
+// order; `f(k, within)` is called for each, within = true when the candidate
+// passed that very test (so a body that tests r^2 < lim2 with the same
+// expression may skip it). Rows whose run exceeds 64 slots are walked directly
+// with the reference's per-cell MAX_CELL_SCAN cap, calling f(k, false) for
+// every candidate of the row (the body then makes its own test).
 template <bool EXACT, class F>
 __device__ __forceinline__ void for_each_within_rows(const SegParams &s, const uint32_t *__restrict__ off,
                                                      const float4 *__restrict__ pos, float4 p, float lim2,
@@ -67,7 +69,7 @@ __device__ __forceinline__ void for_each_within_rows(const SegParams &s, const u
         uint32_t ce = __ldg(&off[row + x + 1]);
         if (ce - cs > (uint32_t)kMaxCellScan) ce = cs + kMaxCellScan;
 #pragma unroll 1
-        for (uint32_t k = cs; k < ce; ++k) f((int)k);
+        for (uint32_t k = cs; k < ce; ++k) f((int)k, false);
       }
       continue;
     }
@@ -84,7 +86,7 @@ __device__ __forceinline__ void for_each_within_rows(const SegParams &s, const u
     while (mm) {
       const int t = __ffsll((long long)mm) - 1;
       mm &= mm - 1ull;
-      f((int)ra + t);
+      f((int)ra + t, true);
     }
   }
 }
@@ -230,7 +232,7 @@ __device__ __forceinline__ void visit_row_masks(const SegParams &s, const uint32
     }
     const int t = __ffsll((long long)m) - 1;
     m &= m - 1ull;
-    f((int)ra + t);
+    f((int)ra + t, true);
   }
 }
 
@@ -328,11 +330,11 @@ struct LambdaAcc {
 
   // Pairs with r2 >= h2 contribute nothing (sph_lambda.glsl:58-62), so the
   // walk may skip them.
-  __device__ __forceinline__ void pair(const SegParams &s, float dx, float dy, float dz, bool self)
+  __device__ __forceinline__ void pair(const SegParams &s, float dx, float dy, float dz, bool self, bool within)
   {
     if (EXACT) {
       const float r2 = dx * dx + dy * dy + dz * dz;
-      if (r2 >= s.h2) return;
+      if (!within && r2 >= s.h2) return;
       density += s.mass * w_poly6(r2, s.h2, s.poly6);
       if (self || r2 <= 1e-12f) return;
       const float r = sqrtf(r2);
@@ -344,7 +346,7 @@ struct LambdaAcc {
       gn2 += ax * ax + ay * ay + az * az;
     } else {
       const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-      if (r2 >= s.h2) return;
+      if (!within && r2 >= s.h2) return;
       const float t = __fsub_rn(s.h2, r2);
       density = __fmaf_rn(__fmul_rn(t, t), t, density);  // scaled by mass * poly6 at the end
       if (self || r2 <= 1e-12f) return;

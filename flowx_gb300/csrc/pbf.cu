@@ -48,9 +48,9 @@ __global__ void __launch_bounds__(512, 3) k_lambda_f(DeviceState d, const float4
   const int3 base = cell_coord(s, pi.x, pi.y, pi.z);
   LambdaAcc<EXACT> acc;
   const MaskRecord rec{d.row_masks, d.row_wide, d.n};
-  for_each_within_recording<EXACT>(s, d.offsets, pred, d.quads, pi, s.h2, base, rec, i, [&](int k) {
+  for_each_within_recording<EXACT>(s, d.offsets, pred, d.quads, pi, s.h2, base, rec, i, [&](int k, bool within) {
     const float4 pj = __ldg(&pred[k]);
-    acc.pair(s, pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, k == i);
+    acc.pair(s, pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, k == i, within);
   });
   const float2 l = acc.finish(s);
   d.lam[i] = l;
@@ -71,12 +71,12 @@ __device__ __forceinline__ float3 delta_sum_f(const SegParams &s, const DeviceSt
   const int3 base = cell_coord(s, pi.x, pi.y, pi.z);
   float ax = 0.0f, ay = 0.0f, az = 0.0f;
   const float h2 = s.h2;
-  auto body = [&](int k) {
+  auto body = [&](int k, bool within) {
     if (k == i) return;
     const float4 pj = RECORDED ? __ldg(&d.plam[k]) : __ldg(&pred[k]);
     const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
     const float r2 = pair_r2<EXACT>(dx, dy, dz);
-    if (r2 >= h2 || r2 <= 1e-12f) return;
+    if ((!within && r2 >= h2) || r2 <= 1e-12f) return;
     delta_pair<EXACT>(s, lambda_i, RECORDED ? pj.w : __ldg(&d.lam[k].y), dx, dy, dz, r2, ax, ay, az);
   };
   if (RECORDED)
@@ -156,12 +156,12 @@ __device__ __forceinline__ float3 xsph_sum_f(const SegParams &s, const DeviceSta
   const bool normals = NORMALS && s.sigma > 0.0f;
   float ax = 0.0f, ay = 0.0f, az = 0.0f;
   float nx = 0.0f, ny = 0.0f, nz = 0.0f, lap = 0.0f;
-  auto body = [&](int k) {
+  auto body = [&](int k, bool within) {
     if (k == i) return;
     const float4 pj = __ldg(&pred[k]);
     const float dx = q.x - pj.x, dy = q.y - pj.y, dz = q.z - pj.z;
     const float r2 = pair_r2<EXACT>(dx, dy, dz);
-    if (r2 >= h2) return;
+    if (!within && r2 >= h2) return;
     float rho_j;
     float3 vj;
     if (QUADS) {
@@ -249,12 +249,12 @@ __global__ void __launch_bounds__(512, 3) k_normal_f(DeviceState d, const float4
   const int3 base = cell_coord(s, pi.x, pi.y, pi.z);
   const float h = s.h, h2 = s.h2, mass = s.mass, poly6m6 = s.poly6m6, vlap = s.visclap;
   float nx = 0.0f, ny = 0.0f, nz = 0.0f, lap = 0.0f;
-  auto body = [&](int k) {
+  auto body = [&](int k, bool within) {
     if (k == i) return;
     const float4 pj = __ldg(&pred[k]);
     const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
     const float r2 = pair_r2<EXACT>(dx, dy, dz);
-    if (r2 >= h2) return;
+    if (!within && r2 >= h2) return;
     const float rho_j = fmaxf(__ldg(&d.lam[k].x), 1e-6f);
     if (EXACT) {
       const float weight = mass / rho_j;
