@@ -329,14 +329,15 @@ struct LambdaAcc {
   float density = 0.0f, gx = 0.0f, gy = 0.0f, gz = 0.0f, gn2 = 0.0f;
 
   // Pairs with r2 >= h2 contribute nothing (sph_lambda.glsl:58-62), so the
-  // walk may skip them.
-  __device__ __forceinline__ void pair(const SegParams &s, float dx, float dy, float dz, bool self, bool within)
+  // walk may skip them. The particle itself (r2 exactly 0) adds its density
+  // and no gradient, which the r2 <= 1e-12 test gives without a test of j == i.
+  __device__ __forceinline__ void pair(const SegParams &s, float dx, float dy, float dz, bool within)
   {
     if (EXACT) {
       const float r2 = dx * dx + dy * dy + dz * dz;
       if (!within && r2 >= s.h2) return;
       density += s.mass * w_poly6(r2, s.h2, s.poly6);
-      if (self || r2 <= 1e-12f) return;
+      if (r2 <= 1e-12f) return;
       const float r = sqrtf(r2);
       const float sg = s.mass * w_spiky_grad(r, s.h, s.spiky);
       const float ax = sg * (dx / r), ay = sg * (dy / r), az = sg * (dz / r);
@@ -349,7 +350,7 @@ struct LambdaAcc {
       if (!within && r2 >= s.h2) return;
       const float t = __fsub_rn(s.h2, r2);
       density = __fmaf_rn(__fmul_rn(t, t), t, density);  // scaled by mass * poly6 at the end
-      if (self || r2 <= 1e-12f) return;
+      if (r2 <= 1e-12f) return;
       const float rinv = rsqrtf(r2);
       const float hr = __fsub_rn(s.h, __fmul_rn(r2, rinv));
       const float g = __fmul_rn(__fmul_rn(s.mass_spiky, __fmul_rn(hr, hr)), rinv);

@@ -50,7 +50,7 @@ __global__ void __launch_bounds__(512, 3) k_lambda_f(DeviceState d, const float4
   const MaskRecord rec{d.row_masks, d.row_wide, d.n};
   for_each_within_recording<EXACT>(s, d.offsets, pred, d.quads, pi, s.h2, base, rec, i, [&](int k, bool within) {
     const float4 pj = __ldg(&pred[k]);
-    acc.pair(s, pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, k == i, within);
+    acc.pair(s, pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, within);
   });
   const float2 l = acc.finish(s);
   d.lam[i] = l;
@@ -72,7 +72,8 @@ __device__ __forceinline__ float3 delta_sum_f(const SegParams &s, const DeviceSt
   float ax = 0.0f, ay = 0.0f, az = 0.0f;
   const float h2 = s.h2;
   auto body = [&](int k, bool within) {
-    if (k == i) return;
+    // j == i needs no test of its own: its r^2 is exactly 0, which the
+    // r^2 <= 1e-12 test below rejects
     const float4 pj = RECORDED ? __ldg(&d.plam[k]) : __ldg(&pred[k]);
     const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
     const float r2 = pair_r2<EXACT>(dx, dy, dz);
