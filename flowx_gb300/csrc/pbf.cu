@@ -109,9 +109,13 @@ __device__ __forceinline__ float4 xsph_input(const SegParams &s, const DeviceSta
 }
 
 // sph_delta.glsl + sph_apply_delta.glsl: pred_out = pred_in + sum / rho0.
-// last: also d.xv[i] for the XSPH pass that follows.
+// last: also d.xv[i] for the XSPH pass that follows. The re-associated form
+// is bounded to four 512-thread blocks per SM (32 registers, no spill): its
+// gathers are latency-bound, and the full 64 resident warps hide more of them
+// (0.726 -> 0.688 ms per launch on the 4M-particle workload); the reference
+// form would spill at 32 and keeps three.
 template <bool EXACT>
-__global__ void __launch_bounds__(512) k_delta_apply_f(DeviceState d, const float4 *__restrict__ pred_in,
+__global__ void __launch_bounds__(512, EXACT ? 3 : 4) k_delta_apply_f(DeviceState d, const float4 *__restrict__ pred_in,
                                                        float4 *__restrict__ pred_out, int last)
 {
   FLOWX_SLOT_PROLOGUE
