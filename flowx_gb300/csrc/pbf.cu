@@ -35,10 +35,11 @@ __device__ __forceinline__ float3 slot_velocity(const float4 &q, const float4 &p
 
 // ---- neighbour passes -------------------------------------------------------
 
-// The neighbour kernels below are bounded to three 512-thread blocks per SM
-// (at most 42 registers): the extra resident warps hide more of the
-// candidate-load latency than the few registers cost (measured 1.6% per
-// frame on the 4M-particle workload).
+// Register bounds of the neighbour kernels below, each measured on the
+// 4M-particle workload: lambda and normal three 512-thread blocks per SM (at
+// most 42 registers: the extra resident warps hide more of the candidate-load
+// latency than the few registers cost, 1.6% per frame), delta_apply four
+// (32), XSPH five 256-thread blocks (48).
 // sph_lambda.glsl:17-77
 template <bool EXACT>
 __global__ void __launch_bounds__(512, 3) k_lambda_f(DeviceState d, const float4 *__restrict__ pred)
@@ -223,9 +224,11 @@ __device__ __forceinline__ float3 xsph_sum_f(const SegParams &s, const DeviceSta
 
 // sph_velocity.glsl + sph_xsph.glsl + sph_finalize.glsl.
 // NORMALS: also the next substep's normals, into d.normal_alt (the slot order
-// of this grid, which the next substep's permute maps to its own).
+// of this grid, which the next substep's permute maps to its own). Bounded to
+// five 256-thread blocks per SM (48 registers): with both bodies it spills at
+// 40 (1.68 -> 1.63 ms per launch on the 4M-particle workload).
 template <bool EXACT, bool NORMALS>
-__global__ void __launch_bounds__(512, 3) k_xsph_finalize_f(DeviceState d, const float4 *__restrict__ pred,
+__global__ void __launch_bounds__(256, 5) k_xsph_finalize_f(DeviceState d, const float4 *__restrict__ pred,
                                                          float4 *__restrict__ pos_out, int keep_delta)
 {
   FLOWX_SLOT_PROLOGUE
