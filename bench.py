@@ -267,6 +267,40 @@ def _oracle_extract(field, surface, verts, tris):
                       "marching cubes; the reference's own is a pure-Python loop)"}
 
 
+def _mesh_voxelizer_metrics(scene, reps=5):
+    """The workload's falling sphere as a triangle mesh (48 x 96 UV sphere,
+    9,024 triangles) voxelised on the device onto its 100^3 collider grid
+    (flowx_voxelize_meshes: the per-frame rebuild the reference does with BVH
+    ray casts on the CPU), wall clock around the call and a synchronise; the
+    oracle's NumPy restatement of the same rule timed once on one thread, and
+    whether the grids agree."""
+    from flowx_gb300 import scenes
+    from flowx_gb300.sph import Solver
+    from oracle import voxelize as oracle_voxelize
+
+    prim = scene.primitives_at(0)[0]
+    verts, tris = scenes.sphere_mesh(prim.r)
+    meshes = [(verts, tris, scenes.translation(*prim.a))]
+    dims, voxel, origin = scene.collider_dims, scene.collider_voxel, scene.config.lo
+    c = scene.config
+    with Solver(c, scene.positions[:8], None, max_cells=c.cell_count,
+                max_collider_voxels=int(np.prod(dims))) as s:
+        s.voxelize_meshes(meshes, dims, voxel, origin)
+        s.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            s.voxelize_meshes(meshes, dims, voxel, origin)
+        s.synchronize()
+        gpu_ms = (time.perf_counter() - t0) / reps * 1e3
+        got = s.collider_occupancy()
+    t0 = time.perf_counter()
+    want = oracle_voxelize.voxelize_meshes(meshes, dims, voxel, origin)
+    cpu_ms = (time.perf_counter() - t0) * 1e3
+    return {"triangles": int(tris.shape[0]), "grid": list(dims), "ms": gpu_ms, "cpu_ms": cpu_ms, "cpu_cores": 1,
+            "matches_oracle": bool(np.array_equal(got, want)), "occupied": int(got.sum()),
+            "timing": "wall clock of Solver.voxelize_meshes (upload, two kernels), synchronised"}
+
+
 def _batched_metrics(substeps=20, warmup=3):
     """The 64-scene batched workload (particle counts log-uniform in
     [2e3, 2e5]): one context stepping all scenes per launch, against the same
@@ -631,6 +665,9 @@ def run_flowx(args):
     if rank == 0 and not args.no_adjoint:
         adjoint = _adjoint_metrics()
     other_configs = _other_configs() if rank == 0 and not args.no_other_configs else None
+    mesh_voxelizer = None
+    if rank == 0 and scene.collider_dims is not None and not args.no_other_configs:
+        mesh_voxelizer = _mesh_voxelizer_metrics(scene)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -680,6 +717,7 @@ def run_flowx(args):
             "batched": batched,
             "adjoint": adjoint,
             "other_configs": other_configs,
+            "mesh_voxelizer": mesh_voxelizer,
             "splat_ms_per_frame": splat_ms,
             "surface_mesh": surface_mesh,
             "splat_samples": samples,

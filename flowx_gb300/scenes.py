@@ -127,6 +127,36 @@ def voxelize(primitives, origin, voxel, dims) -> np.ndarray:
     return occ.astype(np.uint8)
 
 
+def sphere_mesh(radius, rings=48, segments=96):
+    """A closed UV-sphere triangle mesh about the origin (local space), the
+    kind of collider object the reference voxelises: (vertices V x 3 float32,
+    triangles T x 3 int32)."""
+    verts = [(0.0, 0.0, radius)]
+    for i in range(1, rings):
+        th = np.pi * i / rings
+        for j in range(segments):
+            ph = 2.0 * np.pi * j / segments
+            verts.append((radius * np.sin(th) * np.cos(ph), radius * np.sin(th) * np.sin(ph), radius * np.cos(th)))
+    verts.append((0.0, 0.0, -radius))
+    south = len(verts) - 1
+    tris = [(0, 1 + j, 1 + (j + 1) % segments) for j in range(segments)]
+    for i in range(rings - 2):
+        a0, b0 = 1 + i * segments, 1 + (i + 1) * segments
+        for j in range(segments):
+            jn = (j + 1) % segments
+            tris += [(a0 + j, b0 + j, b0 + jn), (a0 + j, b0 + jn, a0 + jn)]
+    last = 1 + (rings - 2) * segments
+    tris += [(last + j, south, last + (j + 1) % segments) for j in range(segments)]
+    return np.asarray(verts, np.float32), np.asarray(tris, np.int32)
+
+
+def translation(x, y, z):
+    """A row-major 4 x 4 world matrix moving local space by (x, y, z)."""
+    m = np.eye(4, dtype=np.float32)
+    m[:3, 3] = (x, y, z)
+    return m
+
+
 def lattice(lo, spacing, counts, h, seed, offset=(0.0, 0.0, 0.0)):
     """Jittered lattice, ids x-fastest. Returns (N, 4) float32 positions, w = 1."""
     nx, ny, nz = counts
