@@ -100,3 +100,22 @@ def test_index_range_is_the_reference_rule():
 
     assert lo == [max(0, math.floor((f[r] - o[r]) / vox)) for r in range(3)]
     assert hi == [min(DIMS[r], math.ceil((g[r] - o[r]) / vox)) for r in range(3)]
+
+
+def test_scene_sphere_mesh_is_closed_and_voxelises_as_the_sphere():
+    """flowx_gb300.scenes.sphere_mesh (the bench's collider mesh): every edge
+    shared by exactly two triangles, and its voxels those of the analytic
+    sphere away from the surface."""
+    from flowx_gb300 import scenes
+
+    v, t = scenes.sphere_mesh(0.3, 24, 48)
+    e = np.sort(np.concatenate([t[:, [0, 1]], t[:, [1, 2]], t[:, [2, 0]]]), axis=1)
+    _, counts = np.unique(e, axis=0, return_counts=True)
+    assert (counts == 2).all()
+    c = (0.05, -0.1, 0.12)
+    g = _grid([(v, t, scenes.translation(*c))])
+    x, y, z = S.centres(DIMS, VOXEL, ORIGIN)
+    d = np.sqrt((x - c[0]) ** 2 + (y - c[1]) ** 2 + (z - c[2]) ** 2)
+    sure = np.abs(d - 0.3) > 0.3 * 0.02
+    assert (d < 0.3)[sure].sum() > 50
+    np.testing.assert_array_equal(g[sure], (d < 0.3)[sure])
