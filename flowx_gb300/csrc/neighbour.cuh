@@ -157,9 +157,8 @@ __device__ __forceinline__ float2 pair_r2_x2(float2 qx, float2 qy, float2 qz, fl
 
 // build_row_masks over the slot quads: the same masks, four candidates per
 // three 16-byte loads. A row [ra, rb) is covered by the quads ra/4 .. (rb-1)/4;
-// quad t's accept bits go to bits 4t..4t+3 of a 68-bit word (ex:hi:lo), whose
-// ra % 4 lowest bits (slots before ra) are then shifted out and whose bits
-// from rb - ra on (slots past the row) are cleared.
+// their accept bits are assembled in order, the ra % 4 bits of slots before
+// ra shifted out and the bits from rb - ra on (slots past the row) cleared.
 template <bool EXACT>
 __device__ __forceinline__ bool build_row_masks_quads(const SegParams &s, const uint32_t *__restrict__ off,
                                                       const SlotQuad *__restrict__ quads, float4 p, float lim2,
@@ -179,27 +178,44 @@ __device__ __forceinline__ bool build_row_masks_quads(const SegParams &s, const 
       const uint32_t len = rb - ra;
       if (len > 64u) return false;
       if (len != 0u) {
-        uint32_t lo = 0u, hi = 0u, ex = 0u;
-        const uint32_t g1 = (rb + 3u) >> 2;
-#pragma unroll 1
-        for (uint32_t g = ra >> 2, sh = 0u; g < g1; ++g, sh += 4u) {
+        const uint32_t lead = ra & 3u;
+        const uint32_t g0 = ra >> 2, g1 = (rb + 3u) >> 2;
+        auto quad_bits = [&](uint32_t g) -> uint32_t {
           const float4 X = __ldg(&quads[g].x), Y = __ldg(&quads[g].y), Z = __ldg(&quads[g].z);
           const float2 a = pair_r2_x2<EXACT>(make_float2(X.x, X.y), make_float2(Y.x, Y.y), make_float2(Z.x, Z.y),
                                              npx, npy, npz);
           const float2 b = pair_r2_x2<EXACT>(make_float2(X.z, X.w), make_float2(Y.z, Y.w), make_float2(Z.z, Z.w),
                                              npx, npy, npz);
-          const uint32_t nib = (a.x < lim2 ? 1u : 0u) | (a.y < lim2 ? 2u : 0u) | (b.x < lim2 ? 4u : 0u) |
-                               (b.y < lim2 ? 8u : 0u);
-          if (sh < 32u)
-            lo |= nib << sh;
-          else if (sh < 64u)
-            hi |= nib << (sh - 32u);
-          else
-            ex = nib;
+          return (a.x < lim2 ? 1u : 0u) | (a.y < lim2 ? 2u : 0u) | (b.x < lim2 ? 4u : 0u) | (b.y < lim2 ? 8u : 0u);
+        };
+        if (lead + len <= 64u) {
+          // at most 16 quads: each enters a 64-bit window (hi:lo) from the
+          // top, so after the last one quad t's bits sit at 64 - 4 (g1 - g0)
+          // + 4 t, and slot ra + s at 64 - 4 (g1 - g0) + lead + s
+          uint32_t lo = 0u, hi = 0u;
+#pragma unroll 1
+          for (uint32_t g = g0; g < g1; ++g) {
+            const uint32_t nib = quad_bits(g);
+            lo = __funnelshift_r(lo, hi, 4);
+            hi = (hi >> 4) | (nib << 28);
+          }
+          mm = (((unsigned long long)hi << 32) | lo) >> (64u - 4u * (g1 - g0) + lead);
+        } else {
+          // 17 quads (a row of 62-64 slots starting off a quad boundary)
+          uint32_t lo = 0u, hi = 0u, ex = 0u;
+#pragma unroll 1
+          for (uint32_t g = g0, sh = 0u; g < g1; ++g, sh += 4u) {
+            const uint32_t nib = quad_bits(g);
+            if (sh < 32u)
+              lo |= nib << sh;
+            else if (sh < 64u)
+              hi |= nib << (sh - 32u);
+            else
+              ex = nib;
+          }
+          mm = (((unsigned long long)hi << 32) | lo) >> lead;
+          mm |= (unsigned long long)ex << (64u - lead);
         }
-        mm = ((unsigned long long)hi << 32) | lo;
-        const uint32_t lead = ra & 3u;
-        if (lead != 0u) mm = (mm >> lead) | ((unsigned long long)ex << (64u - lead));
         if (len < 64u) mm &= (1ull << len) - 1ull;
       }
     }
