@@ -30,7 +30,7 @@ namespace flowx {
 constexpr int kMaxCellScan = 512;       // shaders/sph_common.glsl:30
 constexpr int kMaxColliderSearch = 2;   // shaders/sph_finalize.glsl:13
 constexpr int kSurfaceCellRadius = 2;   // shaders/surface_splat.glsl:30
-constexpr int kSmallCellSort = 32;      // cells above this go to the block sorter
+constexpr int kSmallCellSort = 64;      // cells above this go to the block sorter
 // Cells above this keep the scatter's order instead of the (cell, id) order:
 // the block sorter is quadratic in a cell's size, and such cells only arise
 // from degenerate states (e.g. a blown-up run whose NaN positions all map to

@@ -9,10 +9,12 @@
 //                     (three launches: tile sums, top-level scan, tile scan);
 //                     counters are re-zeroed on the way, cells holding more
 //                     than kSmallCellSort particles are listed;
-//   3. scatter      - (id, old slot) to offset[key] + rank;
-//   4. cell_sort    - order each cell by particle id (thread per cell for small
-//                     cells, block per listed large cell), which makes the
-//                     result the deterministic (cell, id) order;
+//   3. scatter      - (id, old slot) to offset[key] + rank, in a scratch copy;
+//   4. cell_sort    - order each cell by particle id: every pair of a cell of
+//                     at most kSmallCellSort particles counts the smaller pairs
+//                     of its cell and moves to that rank (thread per slot), a
+//                     block ranks each listed large cell; the result is the
+//                     deterministic (cell, id) order;
 //   5. permute      - move particle state into the new slot order.
 //
 // The sorted key column, the [start, end) of every cell and each cell's
@@ -209,7 +211,7 @@ __global__ void k_scatter(DeviceState d)
   if (k >= d.n) return;
   const uint32_t key = d.key_tmp[k];
   const uint32_t slot = d.offsets[key] + d.rank_tmp[k];
-  d.pairs[slot] = ((unsigned long long)d.ids[k] << 32) | (unsigned long long)(uint32_t)k;
+  d.pairs_tmp[slot] = ((unsigned long long)d.ids[k] << 32) | (unsigned long long)(uint32_t)k;
 }
 
 void launch_scatter(const DeviceState &d, cudaStream_t st)
@@ -219,70 +221,50 @@ void launch_scatter(const DeviceState &d, cudaStream_t st)
 }
 
 // ---- 4. order each cell by id -------------------------------------------
-// Small cells: one thread sorts its cell's (id, slot) pairs in registers with
-// an odd-even transposition network of the smallest width in {4, 8, 16, 32}
-// that holds the cell (data-independent control flow keeps the array in
-// registers; padding ~0 sorts last).
-template <int W>
-__device__ __forceinline__ void sort_cell_net(unsigned long long *__restrict__ pairs, uint32_t a, uint32_t n)
+// Cells of at most kSmallCellSort particles: each slot's (id, old slot) pair
+// counts the smaller pairs of its cell in the scatter's copy (ids are unique,
+// so the counts are a permutation of the cell's ranks) and moves there. A
+// warp's slots mostly share one cell, whose pairs its loads then share.
+__global__ void k_cell_rank(DeviceState d)
 {
-  unsigned long long v[W];
-#pragma unroll
-  for (int j = 0; j < W; ++j) v[j] = (uint32_t)j < n ? pairs[a + j] : ~0ull;
-#pragma unroll
-  for (int round = 0; round < W; ++round) {
-#pragma unroll
-    for (int j = round & 1; j + 1 < W; j += 2) {
-      const unsigned long long x = v[j], y = v[j + 1];
-      v[j] = x < y ? x : y;
-      v[j + 1] = x < y ? y : x;
-    }
-  }
-#pragma unroll
-  for (int j = 0; j < W; ++j)
-    if ((uint32_t)j < n) pairs[a + j] = v[j];
-}
-
-__global__ void k_cell_sort_small(DeviceState d)
-{
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= d.cells) return;
-  const uint32_t a = d.offsets[c];
-  const uint32_t n = d.offsets[c + 1] - a;
-  if (n < 2u) return;
-  if (n <= 4u) sort_cell_net<4>(d.pairs, a, n);
-  else if (n <= 8u) sort_cell_net<8>(d.pairs, a, n);
-  else if (n <= 16u) sort_cell_net<16>(d.pairs, a, n);
-  else if (n <= (uint32_t)kSmallCellSort) sort_cell_net<32>(d.pairs, a, n);
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= d.n) return;
+  const unsigned long long pr = d.pairs_tmp[k];
+  const uint32_t cell = __ldg(&d.key_tmp[(uint32_t)pr]);
+  const uint32_t a = __ldg(&d.offsets[cell]);
+  const uint32_t n = __ldg(&d.offsets[cell + 1]) - a;
+  if (n > (uint32_t)kSmallCellSort) return;  // listed: k_cell_sort_large
+  uint32_t rank = 0;
+  for (uint32_t f = 0; f < n; ++f) rank += __ldg(&d.pairs_tmp[a + f]) < pr ? 1u : 0u;
+  d.pairs[a + rank] = pr;
 }
 
 // Large cells (listed by the scan): a block ranks each element against all
-// others of its cell (ids are unique, so ranks are a permutation), writes to
-// the scratch copy and copies back. O(n^2 / blockDim) per cell, so cells
-// above kMaxRankSortCell are left in the scatter's order.
+// others of its cell, from the scatter's copy into place. O(n^2 / blockDim)
+// per cell, so cells above kMaxRankSortCell keep the scatter's order.
 __global__ void __launch_bounds__(256) k_cell_sort_large(DeviceState d)
 {
   const uint32_t count = d.big_cells[0];
   for (uint32_t item = blockIdx.x; item < count; item += gridDim.x) {
     const uint32_t c = d.big_cells[1 + item];
     const uint32_t a = d.offsets[c], n = d.offsets[c + 1] - a;
-    if (n > (uint32_t)kMaxRankSortCell) continue;  // uniform across the block
-    for (uint32_t e = threadIdx.x; e < n; e += blockDim.x) {
-      const unsigned long long mine = d.pairs[a + e];
-      uint32_t rank = 0;
-      for (uint32_t f = 0; f < n; ++f) rank += d.pairs[a + f] < mine ? 1u : 0u;
-      d.pairs_tmp[a + rank] = mine;
+    if (n > (uint32_t)kMaxRankSortCell) {  // uniform across the block
+      for (uint32_t e = threadIdx.x; e < n; e += blockDim.x) d.pairs[a + e] = d.pairs_tmp[a + e];
+      continue;
     }
-    __syncthreads();
-    for (uint32_t e = threadIdx.x; e < n; e += blockDim.x) d.pairs[a + e] = d.pairs_tmp[a + e];
-    __syncthreads();
+    for (uint32_t e = threadIdx.x; e < n; e += blockDim.x) {
+      const unsigned long long mine = d.pairs_tmp[a + e];
+      uint32_t rank = 0;
+      for (uint32_t f = 0; f < n; ++f) rank += d.pairs_tmp[a + f] < mine ? 1u : 0u;
+      d.pairs[a + rank] = mine;
+    }
   }
 }
 
 void launch_cell_sort(const DeviceState &d, cudaStream_t st)
 {
-  const int b = FLOWX_BLOCK(d, K_CELL_SORT_SMALL, 128, k_cell_sort_small);
-  if (d.cells > 0) k_cell_sort_small<<<grid_for(d.cells, b), b, 0, st>>>(d);
+  const int b = FLOWX_BLOCK(d, K_CELL_SORT_SMALL, 256, k_cell_rank);
+  if (d.n > 0) k_cell_rank<<<grid_for(d.n, b), b, 0, st>>>(d);
   k_cell_sort_large<<<d.sm_count, 256, 0, st>>>(d);
 }
 
