@@ -196,7 +196,7 @@ def _oracle_sample(scene, target_s=10.0, max_substeps=4):
     from flowx_gb300 import config as C
     from oracle import oracle as O
 
-    c = scene.config
+    c = dataclasses.replace(scene.config, particle_count=scene.n)
     ic = C.collider_binding(scene.collider_dims, scene.collider_voxel)
     o = O.Oracle(C.push_constant_values(c, scene.dt, ic), scene.positions, scene.velocities,
                  collider=scene.collider_grid(0), iterations=c.iterations)
@@ -282,7 +282,7 @@ def _mesh_voxelizer_metrics(scene, reps=5):
     verts, tris = scenes.sphere_mesh(prim.r)
     meshes = [(verts, tris, scenes.translation(*prim.a))]
     dims, voxel, origin = scene.collider_dims, scene.collider_voxel, scene.config.lo
-    c = scene.config
+    c = dataclasses.replace(scene.config)  # the Solver records its own particle count in its config
     with Solver(c, scene.positions[:8], None, max_cells=c.cell_count,
                 max_collider_voxels=int(np.prod(dims))) as s:
         s.voxelize_meshes(meshes, dims, voxel, origin)
