@@ -39,7 +39,7 @@ struct Ctx {
   uint32_t *d_src_slot = nullptr;  // reorder scratch for key uploads
   void *d_prims = nullptr;         // voxeliser primitives
   int prim_cap = 0;
-  void *d_mesh = nullptr;          // mesh voxeliser scratch (vertices, triangles, world vertices, flips)
+  void *d_mesh = nullptr;          // mesh voxeliser scratch (vertices, triangles, world vertices)
   size_t mesh_cap = 0;
   std::vector<SegParams> segs;
   bool segs_uploaded = false;

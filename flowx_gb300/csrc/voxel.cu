@@ -11,7 +11,7 @@
 // transform voxelises to nothing (:340-353).
 //
 // Here the same parity is counted exactly: world-space triangles in double
-// precision, one thread per (x, y) column of the mesh's range. The vertical
+// precision, one warp per (x, y) column of the mesh's range. The vertical
 // line through a column's centres crosses a triangle when the column point is
 // inside the triangle's projection; the edge tests are watertight: an edge's
 // function is evaluated from its lexicographically smaller endpoint, so the
@@ -19,7 +19,7 @@
 // an edge or vertex is decided as the point displaced by (eps, eps^2) would be
 // (simulation of simplicity), which lies in exactly one triangle of a planar
 // fan. A crossing at height z flips the parity of every centre below z: the
-// thread records flips per crossing and sums them from the top of the column.
+// warp records one flip bit per crossing and counts them from the top.
 // Triangles with no projected area cannot be crossed transversally and are
 // skipped.
 #include <algorithm>
@@ -81,21 +81,30 @@ __device__ __forceinline__ int centres_below(double z, double oz, double voxel, 
   return k - k0;
 }
 
+// One warp per column: the lanes share the column's triangles, and each
+// crossing toggles bit m (the number of centres below it) of the column's
+// flip set in shared memory; the XOR of toggles commutes, so the result does
+// not depend on which lane finds which crossing. Voxel r of the column is
+// inside when the bits above r hold an odd count.
 __global__ void k_mesh_columns(const double *__restrict__ w, const int32_t *__restrict__ tri, int ntri, int i0, int i1,
                                int j0, int j1, int k0, int k1, int nx, int ny, double ox, double oy, double oz,
-                               double voxel, uint8_t *__restrict__ flips, uint8_t *__restrict__ grid)
+                               double voxel, uint8_t *__restrict__ grid)
 {
-  const int ci = blockIdx.x * blockDim.x + threadIdx.x;
+  extern __shared__ uint32_t column_flips[];
+  const int ci = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // warp-uniform
+  const int lane = threadIdx.x & 31;
   const int ncol_x = i1 - i0;
   const int ncol = ncol_x * (j1 - j0);
   if (ci >= ncol) return;
   const int i = i0 + ci % ncol_x, j = j0 + ci / ncol_x;
   const int nzr = k1 - k0;
-  uint8_t *f = flips + (size_t)ci * (nzr + 1);
-  for (int m = 0; m <= nzr; ++m) f[m] = 0;
+  const int words = (nzr + 1 + 31) >> 5;
+  uint32_t *f = column_flips + (threadIdx.x >> 5) * words;
+  for (int q = lane; q < words; q += 32) f[q] = 0u;
+  __syncwarp();
   const double px = ox + ((double)i + 0.5) * voxel;
   const double py = oy + ((double)j + 0.5) * voxel;
-  for (int t = 0; t < ntri; ++t) {
+  for (int t = lane; t < ntri; t += 32) {
     const int ia = tri[3 * t], ib = tri[3 * t + 1], ic = tri[3 * t + 2];
     double ax = w[3 * ia], ay = w[3 * ia + 1], az = w[3 * ia + 2];
     double bx = w[3 * ib], by = w[3 * ib + 1], bz = w[3 * ib + 2];
@@ -117,12 +126,16 @@ __global__ void k_mesh_columns(const double *__restrict__ w, const int32_t *__re
     const double wc = edge_fn(ax, ay, bx, by, px, py);
     if (!edge_in(wc, ax, ay, bx, by)) continue;
     const double z = ((wa * az + wb * bz) + wc * cz) / ((wa + wb) + wc);
-    f[centres_below(z, oz, voxel, k0, k1)] ^= 1;
+    const int m = centres_below(z, oz, voxel, k0, k1);
+    atomicXor(&f[m >> 5], 1u << (m & 31));
   }
-  uint8_t inside = 0;
-  for (int r = nzr - 1; r >= 0; --r) {
-    inside ^= f[r + 1];
-    if (inside) grid[((size_t)(k0 + r) * ny + j) * nx + i] = 1;
+  __syncwarp();
+  for (int r = lane; r < nzr; r += 32) {
+    const int m0 = r + 1;  // crossings counted by voxel r: bits m0 .. nzr
+    int q = m0 >> 5;
+    uint32_t count = (uint32_t)__popc(f[q] & (0xffffffffu << (m0 & 31)));
+    for (++q; q < words; ++q) count += (uint32_t)__popc(f[q]);
+    if (count & 1u) grid[((size_t)(k0 + r) * ny + j) * nx + i] = 1;
   }
 }
 
@@ -195,8 +208,7 @@ extern "C" int flowx_voxelize_meshes(flowx_ctx *ctx, const flowx_mesh *meshes, i
     const size_t b_v = align_up(sizeof(float) * 3 * (size_t)m.vertex_count);
     const size_t b_t = align_up(sizeof(int32_t) * 3 * (size_t)m.triangle_count);
     const size_t b_w = align_up(sizeof(double) * 3 * (size_t)m.vertex_count);
-    const size_t b_f = align_up(ncol * (size_t)(hi3[2] - lo3[2] + 1));
-    const size_t need = b_v + b_t + b_w + b_f;
+    const size_t need = b_v + b_t + b_w;
     if (need > c->mesh_cap) {
       rc = c->cuda(cudaStreamSynchronize(c->stream), "mesh scratch resize");
       if (rc) return rc;
@@ -211,7 +223,6 @@ extern "C" int flowx_voxelize_meshes(flowx_ctx *ctx, const flowx_mesh *meshes, i
     float *d_v = reinterpret_cast<float *>(base);
     int32_t *d_t = reinterpret_cast<int32_t *>(base + b_v);
     double *d_w = reinterpret_cast<double *>(base + b_v + b_t);
-    uint8_t *d_f = reinterpret_cast<uint8_t *>(base + b_v + b_t + b_w);
     rc = c->cuda(cudaMemcpyAsync(d_v, m.vertices, sizeof(float) * 3 * (size_t)m.vertex_count, cudaMemcpyHostToDevice,
                                  c->stream),
                  "mesh vertex upload");
@@ -221,9 +232,10 @@ extern "C" int flowx_voxelize_meshes(flowx_ctx *ctx, const flowx_mesh *meshes, i
                    "mesh triangle upload");
     if (rc) return rc;
     k_mesh_world<<<(m.vertex_count + 255) / 256, 256, 0, c->stream>>>(d_v, m.vertex_count, a, d_w);
-    k_mesh_columns<<<(unsigned)((ncol + 127) / 128), 128, 0, c->stream>>>(
+    const int words = (hi3[2] - lo3[2] + 1 + 31) / 32;  // a column's flip bits, per warp
+    k_mesh_columns<<<(unsigned)((ncol + 3) / 4), 128, (size_t)4 * words * sizeof(uint32_t), c->stream>>>(
         d_w, d_t, m.triangle_count, lo3[0], hi3[0], lo3[1], hi3[1], lo3[2], hi3[2], dims[0], dims[1], ox, oy, oz, vox,
-        d_f, c->d.collider);
+        c->d.collider);
     g_launches += 2;
     // the next mesh's uploads reuse the scratch after these kernels (stream order)
   }
