@@ -747,6 +747,8 @@ def main():
     ap.add_argument("--case", action="store_true",
                     help="untimed launch-by-launch run of --warmup frames, for profiler captures")
     ap.add_argument("--exact", action="store_true", help="with --case: the reference's float expressions")
+    ap.add_argument("--surface", action="store_true",
+                    help="with --case: then the frame's surface twice (splat and marching cubes)")
     args = ap.parse_args()
     if args.warmup < 3:
         print("bench.py: --warmup below 3 is raised to 3", file=sys.stderr)
@@ -773,7 +775,7 @@ def run_case(args):
     c = scene.config
     sol = Solver(c, scene.positions, scene.velocities, max_cells=c.cell_count,
                  max_collider_voxels=int(np.prod(scene.collider_dims)) if scene.collider_dims else 0,
-                 exact=args.exact)
+                 max_surface_samples=scene.surface.sample_count if args.surface else 0, exact=args.exact)
     if scene.collider_dims is not None:
         sol.voxelize(scene.primitives_at(0), scene.collider_dims, scene.collider_voxel)
     sol._build_grid(0.0)
@@ -782,6 +784,9 @@ def run_case(args):
             sol.voxelize(scene.primitives_at(f), scene.collider_dims, scene.collider_voxel)
         for _ in range(scene.substeps_per_frame):
             sol._substep(scene.dt)
+    if args.surface:
+        for _ in range(2):
+            sol.surface_mesh(scene.surface, scene.dt)
     ok = bool(np.isfinite(sol.read("positions")).all())
     sol.close()
     print(json.dumps({"case": scene.name, "frames": args.warmup, "finite": ok}))
