@@ -242,24 +242,41 @@ __device__ __forceinline__ long long lattice_edge(const Lattice &L, const McTabl
   return sample_index(L, i + cx, j + cy, k + cz) * 3 + t.walk[e][2];
 }
 
+// Also lists the cubes with triangles (the only ones with owned crossed edges
+// or triangles to emit) for the vertex and triangle kernels, one atomic per
+// warp; the list's order does not matter, every output position comes from
+// the scans.
 __global__ void __launch_bounds__(kMcBlock) k_mc_classify(const float *__restrict__ field, Lattice L,
                                                           const McTables *__restrict__ t,
-                                                          uint8_t *__restrict__ cases, uint2 *__restrict__ counts)
+                                                          uint8_t *__restrict__ cases, uint2 *__restrict__ counts,
+                                                          uint32_t *__restrict__ active, uint32_t *__restrict__ nactive)
 {
   const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= cube_count(L)) return;
-  int i, j, k;
-  cube_coord(L, c, i, j, k);
-  const long long base = sample_index(L, i, j, k);
-  const long long nx = L.nx, nxy = (long long)L.nx * L.ny;
-  const long long off[8] = {0, 1, 1 + nx, nx, nxy, 1 + nxy, 1 + nx + nxy, nx + nxy};
-  int cs = 0;
+  const bool in = c < cube_count(L);
+  int nt = 0;
+  if (in) {
+    int i, j, k;
+    cube_coord(L, c, i, j, k);
+    const long long base = sample_index(L, i, j, k);
+    const long long nx = L.nx, nxy = (long long)L.nx * L.ny;
+    const long long off[8] = {0, 1, 1 + nx, nx, nxy, 1 + nxy, 1 + nx + nxy, nx + nxy};
+    int cs = 0;
 #pragma unroll
-  for (int q = 0; q < 8; ++q)
-    if ((double)__ldg(&field[base + off[q]]) >= L.iso) cs |= 1 << q;
-  cases[c] = (uint8_t)cs;
-  const int flags = (i == 0 ? 1 : 0) | (j == 0 ? 2 : 0) | (k == 0 ? 4 : 0);
-  counts[c] = make_uint2((uint32_t)t->ntri[cs], (uint32_t)__popc((unsigned)(t->crossed[cs] & t->owned[flags])));
+    for (int q = 0; q < 8; ++q)
+      if ((double)__ldg(&field[base + off[q]]) >= L.iso) cs |= 1 << q;
+    cases[c] = (uint8_t)cs;
+    const int flags = (i == 0 ? 1 : 0) | (j == 0 ? 2 : 0) | (k == 0 ? 4 : 0);
+    nt = t->ntri[cs];
+    counts[c] = make_uint2((uint32_t)nt, (uint32_t)__popc((unsigned)(t->crossed[cs] & t->owned[flags])));
+  }
+  const unsigned ballot = __ballot_sync(0xffffffffu, nt > 0);
+  if (ballot) {
+    const int lane = threadIdx.x & 31, leader = __ffs((int)ballot) - 1;
+    uint32_t slot = 0;
+    if (lane == leader) slot = atomicAdd(nactive, (uint32_t)__popc(ballot));
+    slot = __shfl_sync(0xffffffffu, slot, leader);
+    if (nt > 0) active[slot + (uint32_t)__popc(ballot & ((1u << lane) - 1u))] = (uint32_t)c;
+  }
 }
 
 // ---- exclusive scan of the (triangles, vertices) pairs ----------------------
@@ -358,16 +375,19 @@ __global__ void __launch_bounds__(kMcBlock) k_mc_tile_scan(uint2 *__restrict__ i
   }
 }
 
-// solver/marching_cubes.py:258-276 for the edges a cube owns, in first-use order.
+// solver/marching_cubes.py:258-276 for the edges a cube owns, in first-use
+// order; one thread per listed cube.
 __global__ void __launch_bounds__(kMcBlock) k_mc_vertices(const float *__restrict__ field, Lattice L,
                                                           const McTables *__restrict__ t,
                                                           const uint8_t *__restrict__ cases,
                                                           const uint2 *__restrict__ base_of,
+                                                          const uint32_t *__restrict__ active, uint32_t nactive,
                                                           uint32_t *__restrict__ edge_vertex,
                                                           double *__restrict__ vertices)
 {
-  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= cube_count(L)) return;
+  const long long a = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= nactive) return;
+  const long long c = active[a];
   const int cs = cases[c];
   if (cs == 0 || cs == 255) return;
   int i, j, k;
@@ -405,11 +425,13 @@ __global__ void __launch_bounds__(kMcBlock) k_mc_vertices(const float *__restric
 __global__ void __launch_bounds__(kMcBlock) k_mc_triangles(Lattice L, const McTables *__restrict__ t,
                                                            const uint8_t *__restrict__ cases,
                                                            const uint2 *__restrict__ base_of,
+                                                           const uint32_t *__restrict__ active, uint32_t nactive,
                                                            const uint32_t *__restrict__ edge_vertex,
                                                            int32_t *__restrict__ triangles)
 {
-  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= cube_count(L)) return;
+  const long long a = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= nactive) return;
+  const long long c = active[a];
   const int cs = cases[c];
   const int nt = t->ntri[cs];
   if (nt == 0) return;
@@ -430,9 +452,11 @@ struct MarchingCubes {
   uint8_t *cases = nullptr;
   uint2 *counts = nullptr, *tile_sums = nullptr, *grand = nullptr;
   uint32_t *edge_vertex = nullptr;
+  uint32_t *active = nullptr, *nactive = nullptr;  // cubes with triangles, and how many
   double *vertices = nullptr;
   int32_t *triangles = nullptr;
   long long cap_cubes = 0, cap_counts = 0, cap_tiles = 0, cap_edges = 0, cap_vertices = 0, cap_triangles = 0;
+  long long cap_active = 0;
   long long nvert = 0, ntri = 0;
   cudaStream_t last_stream = nullptr;
 
@@ -459,7 +483,7 @@ struct MarchingCubes {
   }
   void release()
   {
-    void *ptrs[] = {d_tables, cases, counts, tile_sums, grand, edge_vertex, vertices, triangles};
+    void *ptrs[] = {d_tables, cases, counts, tile_sums, grand, edge_vertex, vertices, triangles, active, nactive};
     for (void *p : ptrs)
       if (p) cudaFree(p);
   }
@@ -506,6 +530,7 @@ int flowx_mc_create(int32_t device, flowx_mc **out)
   if (!rc) rc = m->cuda(cudaMalloc((void **)&m->d_tables, sizeof(McTables)), "table allocation");
   if (!rc) rc = m->cuda(cudaMemcpy(m->d_tables, t, sizeof(McTables), cudaMemcpyHostToDevice), "table upload");
   if (!rc) rc = m->cuda(cudaMalloc((void **)&m->grand, sizeof(uint2)), "allocation");
+  if (!rc) rc = m->cuda(cudaMalloc((void **)&m->nactive, sizeof(uint32_t)), "allocation");
   if (rc) {
     g_mc_create_error = m->err;
     m->release();
@@ -521,7 +546,8 @@ int flowx_mc_destroy(flowx_mc *mc)
   if (!mc) return FLOWX_OK;
   MarchingCubes *m = as_mc(mc);
   cudaSetDevice(m->device);
-  if (m->last_stream) cudaStreamSynchronize(m->last_stream);
+  // The last extraction ran on the caller's stream, which may already be
+  // destroyed: cudaFree itself waits for the device's outstanding work.
   m->release();
   delete m;
   return FLOWX_OK;
@@ -557,25 +583,34 @@ int flowx_mc_extract(flowx_mc *mc, const float *field, const int32_t dims[3], co
   if (!rc) rc = m->grow(&m->counts, m->cap_counts, cubes, "count buffer");
   if (!rc) rc = m->grow(&m->tile_sums, m->cap_tiles, tiles, "scan buffer");
   if (!rc) rc = m->grow(&m->edge_vertex, m->cap_edges, samples * 3, "edge buffer");
+  if (!rc) rc = m->grow(&m->active, m->cap_active, cubes, "active cube list");
+  if (!rc) rc = m->cuda(cudaMemsetAsync(m->nactive, 0, sizeof(uint32_t), st), "active count reset");
   if (rc) return rc;
   Lattice L{dims[0], dims[1], dims[2], origin[0], origin[1], origin[2], spacing, iso};
   const unsigned nb = (unsigned)((cubes + kMcBlock - 1) / kMcBlock);
-  k_mc_classify<<<nb, kMcBlock, 0, st>>>(field, L, m->d_tables, m->cases, m->counts);
+  k_mc_classify<<<nb, kMcBlock, 0, st>>>(field, L, m->d_tables, m->cases, m->counts, m->active, m->nactive);
   k_mc_tile_sums<<<(unsigned)tiles, kMcBlock, 0, st>>>(m->counts, cubes, m->tile_sums);
   k_mc_scan_sums<<<1, kMcBlock, 0, st>>>(m->tile_sums, (int)tiles, m->grand);
   k_mc_tile_scan<<<(unsigned)tiles, kMcBlock, 0, st>>>(m->counts, cubes, m->tile_sums);
   uint2 totals{0, 0};
+  uint32_t nactive = 0;
   rc = m->cuda(cudaMemcpyAsync(&totals, m->grand, sizeof(uint2), cudaMemcpyDeviceToHost, st), "count read-back");
+  if (!rc)
+    rc = m->cuda(cudaMemcpyAsync(&nactive, m->nactive, sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
+                 "count read-back");
   if (!rc) rc = m->cuda(cudaStreamSynchronize(st), "marching cubes count");
   if (rc) return rc;
   g_launches += 4;
   rc = m->grow(&m->vertices, m->cap_vertices, 3 * (long long)totals.y, "vertex buffer");
   if (!rc) rc = m->grow(&m->triangles, m->cap_triangles, 3 * (long long)totals.x, "triangle buffer");
   if (rc) return rc;
+  const unsigned na = (unsigned)((nactive + kMcBlock - 1) / kMcBlock);
   if (totals.y > 0)
-    k_mc_vertices<<<nb, kMcBlock, 0, st>>>(field, L, m->d_tables, m->cases, m->counts, m->edge_vertex, m->vertices);
+    k_mc_vertices<<<na, kMcBlock, 0, st>>>(field, L, m->d_tables, m->cases, m->counts, m->active, nactive,
+                                           m->edge_vertex, m->vertices);
   if (totals.x > 0)
-    k_mc_triangles<<<nb, kMcBlock, 0, st>>>(L, m->d_tables, m->cases, m->counts, m->edge_vertex, m->triangles);
+    k_mc_triangles<<<na, kMcBlock, 0, st>>>(L, m->d_tables, m->cases, m->counts, m->active, nactive, m->edge_vertex,
+                                            m->triangles);
   g_launches += 2;
   rc = m->cuda(cudaGetLastError(), "flowx_mc_extract");
   if (rc) return rc;

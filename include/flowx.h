@@ -350,7 +350,9 @@ int flowx_mc_create(int32_t device, flowx_mc **out);
 int flowx_mc_destroy(flowx_mc *mc);
 const char *flowx_mc_last_error(const flowx_mc *mc);
 /* Extract on `stream` (NULL = default stream; it is synchronised for the
- * counts). field: device pointer, dims[0] * dims[1] * dims[2] floats. */
+ * counts). field: device pointer, dims[0] * dims[1] * dims[2] floats. The
+ * stream must stay valid until flowx_mc_download / flowx_mc_mesh of this
+ * extraction (they order on it); flowx_mc_destroy does not use it. */
 int flowx_mc_extract(flowx_mc *mc, const float *field, const int32_t dims[3], const double origin[3], double spacing,
                      double iso, void *stream, int64_t *vertex_count, int64_t *triangle_count);
 /* The last extraction to host: vertices V x 3 doubles, triangles T x 3 int32. */
