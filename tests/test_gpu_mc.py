@@ -133,3 +133,21 @@ def test_solver_surface_mesh_matches_oracle_pool():
     assert len(ot) > 10000
     np.testing.assert_array_equal(tris, ot)
     np.testing.assert_array_equal(verts, ov)
+
+
+def test_destroy_after_the_extraction_stream_is_gone():
+    """An extraction on a solver's stream, the solver closed first (its stream
+    destroyed), then the marching-cubes object: destroy must not use the
+    caller's stream of the last extraction."""
+    from flowx_gb300 import scenes
+    from flowx_gb300.sph import Solver
+    from flowx_gb300.surface import MarchingCubes
+
+    sc = scenes.dam_break()
+    mc = MarchingCubes(0)
+    s = Solver(sc.config, sc.positions, sc.velocities, max_surface_samples=sc.surface.sample_count)
+    s._build_grid(0.0)
+    verts, tris = s.surface_mesh(sc.surface, sc.dt, mc)
+    assert len(tris) > 0
+    s.close()
+    mc.close()
