@@ -60,3 +60,23 @@ def test_reference_arm_non_zero_rank_exits_without_work():
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
                         "--warmup", "3"], capture_output=True, text=True, env=env, timeout=120)
     assert r.returncode == 0 and r.stdout.strip() == ""
+
+
+def test_cpu_samples_report_their_own_workload():
+    """The CPU baseline helpers on a small scene: a positive rate over the
+    scene's own particle count, the threads used, and the one-thread sample
+    on a column of the same fluid."""
+    sys.path.insert(0, ROOT)
+    import bench
+    from flowx_gb300 import scenes
+    from oracle import oracle as O
+
+    O.build()
+    sc = scenes.dam_break()
+    sc.config.particle_count = 8  # a Solver elsewhere may have recorded its own count
+    r = bench._oracle_sample(sc, target_s=0.05, max_substeps=1)
+    assert r["value"] > 0 and r["cores"] >= 1 and r["kind"] == "port"
+    assert f"{sc.n}-particle" in r["sample"]
+    one = r["one_core"]
+    assert one["cores"] == 1 and one["value"] > 0
+    assert O.max_threads() == r["cores"]  # the thread count is restored
