@@ -18,10 +18,13 @@
  *    them out) and one R32F 3-D image; out-of-range loads return 0 and
  *    out-of-range stores are dropped, as GLSL image access does;
  *  - floatBitsToInt / intBitsToFloat bit casts.
- * One deliberate difference: unsuffixed literals such as 0.4 are double in
- * C++ and float in GLSL, so mixed expressions round once more at the end. The
- * harness is compiled with -ffp-contract=off; the difference is at the level
- * of one float ulp per expression.
+ * Unsuffixed literals such as 0.4 are double in C++ and float in GLSL: the
+ * harness is compiled with -fsingle-precision-constant (and -ffp-contract=off),
+ * so they are float here too and every expression rounds as the shader
+ * writes it. pow() is glibc's powf, correctly rounded; GLSL leaves pow's
+ * precision to the implementation (it inherits exp2(y * log2(x))'s), so an
+ * integer power such as sph_delta.glsl's pow(ratio, 4.0) may differ by an
+ * ulp from a restatement that squares twice.
  */
 
 /* ---- scalar builtins -------------------------------------------------- */

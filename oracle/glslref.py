@@ -86,8 +86,12 @@ class Images(ctypes.Structure):
     ]
 
 
-def build(ref_root="/root/reference"):
-    """Compile the harness from the reference checkout (oracle/glsl_cpu/Makefile)."""
+def build(ref_root=None):
+    """Compile the harness from the reference checkout (oracle/glsl_cpu/Makefile);
+    ``ref_root`` defaults to ``oracle.refpath.checkout()``."""
+    from oracle import refpath
+
+    ref_root = ref_root or refpath.checkout()
     subprocess.run(
         ["make", "-s", "-C", os.path.join(HERE, "glsl_cpu"), f"REF={ref_root}"],
         check=True,

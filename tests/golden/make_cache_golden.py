@@ -6,7 +6,7 @@ f at header_size + (f - seed_frame - 1) * frame_size, positions then
 velocities as little-endian f32, the header rewritten with last_frame after
 every frame). Run where the reference checkout is mounted:
 
-    python tests/golden/make_cache_golden.py [--ref /root/reference]
+    python tests/golden/make_cache_golden.py [--ref CHECKOUT]
 
 Stored: the inputs (header fields, per-frame arrays) and the file bytes after
 each frame write (checked against the reference's ``_unpack_header``).
@@ -24,14 +24,17 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
 import reference_host  # noqa: E402
+from oracle import refpath  # noqa: E402
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=None, help="reference checkout (default: $FLOWX_REFERENCE)")
     args = ap.parse_args()
+    args.ref = args.ref or refpath.checkout()
     reference_host.load(args.ref)
     cache = importlib.import_module("flowx_reference.solver.cache")
 

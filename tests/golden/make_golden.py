@@ -2,7 +2,7 @@
 
 Run where the reference checkout is mounted (it is read, never modified):
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py [--ref CHECKOUT]
 
 Two kinds of fixtures:
 
@@ -38,6 +38,7 @@ sys.path.insert(0, HERE)
 from flowx_gb300 import config as C  # noqa: E402
 from flowx_gb300 import scenes  # noqa: E402
 from oracle import glslref as G  # noqa: E402
+from oracle import refpath  # noqa: E402
 
 
 # ---------------------------------------------------------------- host vectors
@@ -207,8 +208,9 @@ def pile_scene():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=None, help="reference checkout (default: $FLOWX_REFERENCE)")
     args = ap.parse_args()
+    args.ref = args.ref or refpath.checkout()
     G.build(args.ref)
     host_vectors(args.ref)
     trace_scene("dam_break", scenes.dam_break(), substeps=4, splat_dims=64)

@@ -2,7 +2,7 @@
 cubes (``solver/marching_cubes.py``, pure Python, imported from the reference
 checkout, which is read and never modified):
 
-    python tests/golden/make_mc_golden.py [--ref /root/reference]
+    python tests/golden/make_mc_golden.py [--ref CHECKOUT]
 
 Contents:
 
@@ -36,6 +36,7 @@ sys.path.insert(0, ROOT)
 
 from flowx_gb300 import config as C  # noqa: E402
 from flowx_gb300 import scenes  # noqa: E402
+from oracle import refpath  # noqa: E402
 
 
 def _fields():
@@ -68,8 +69,9 @@ def _fields():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=None, help="reference checkout (default: $FLOWX_REFERENCE)")
     args = ap.parse_args()
+    args.ref = args.ref or refpath.checkout()
     sys.path.insert(0, os.path.join(args.ref, "solver"))
     import marching_cubes as mc  # the reference module
 

@@ -1,13 +1,15 @@
 """The C restatement (oracle/pbf_oracle.c) pinned against the reference's own
 GLSL passes (golden traces in tests/golden/, generated by make_golden.py from
-the reference's shader source compiled for the CPU).
+the reference's shader source compiled for the CPU with float literals, as
+GLSL has them).
 
 Pass by pass: each pass of the first substep is run on exactly the inputs the
 reference's pass saw (the trace's state, updated with the trace's own outputs
-as it goes), so each comparison isolates one pass. Integer work (keys, cell
-ranges) must be bit-exact; float outputs must agree to a few float32 ulps of
-the buffer's scale (the oracle rounds constants in float32, the reference
-harness in double).
+as it goes), so each comparison isolates one pass. Every pass is bit-exact
+except delta, whose pow(ratio, 4.0) (sph_delta.glsl:75) the harness takes
+from glibc's powf and the oracle from two squarings: GLSL leaves pow's
+precision to the implementation, and the two differ by about an ulp of a term
+(at most 2e-7 of the buffer's scale on these scenes).
 """
 
 import numpy as np
@@ -20,10 +22,8 @@ PASS_IDS = {
     "normal": O.NORMAL, "predict": O.PREDICT, "lambda": O.LAMBDA, "delta": O.DELTA,
     "apply_delta": O.APPLY_DELTA, "velocity": O.VELOCITY, "xsph": O.XSPH, "finalize": O.FINALIZE,
 }
-# Scale-relative tolerance per pass. The normal pass sums weights of
-# mass/max(rho, 1e-6) whose terms cancel; 1e-5 of the buffer scale still
-# bounds it well inside float32 behaviour.
-REL = {"normal": 2e-5, "lambda": 2e-5}
+# Scale-relative tolerance of the one pass that is not bit-exact (see above).
+DELTA_REL = 1e-6
 
 
 def _oracle(tr):
@@ -50,7 +50,11 @@ def test_oracle_passes_match_reference(scene):
             o.run_pass(PASS_IDS[name], o.push(dt))
             for b, want in outs.items():
                 got = getattr(o, "lambda_" if b == "lambda" else b)
-                assert_close(f"{scene} pass {idx} {name}.{b}", got, want, rel=REL.get(name, 1e-5))
+                tag = f"{scene} pass {idx} {name}.{b}"
+                if name == "delta":
+                    assert_close(tag, got, want, rel=DELTA_REL)
+                else:
+                    np.testing.assert_array_equal(got, want, err_msg=tag)
         # continue from the reference's own outputs
         o.load(outs)
 
@@ -76,12 +80,13 @@ def test_oracle_stable_grid_matches_reference_membership(scene):
         assert list(o.keys[s:e, 1].astype(int)) == ids
 
 
-@pytest.mark.parametrize("scene", ["dam_break", "pool_small"])
+@pytest.mark.parametrize("scene", ["dam_break", "pool_small", "pile"])
 def test_oracle_substep_matches_reference(scene):
-    """A whole first substep from the seeded state, bitonic order, against the
-    reference. Bounded by 1e-4 h: with cohesion on, curvature is -lap/|n| with
-    |n| a cancelling sum, which turns one-ulp differences in the kernel
-    constants into ~5e-5 h after one substep (measured; see DESIGN)."""
+    """A whole first substep from the seeded state (cohesion on), bitonic
+    order, against the reference: positions within 1e-5 h (measured 6e-7 to
+    1.2e-6 h; the delta pass's ulp is all that differs). The scene at the
+    reference's own parameters flies apart within the substep and is held to
+    the per-pass comparison only."""
     tr = Trace(scene)
     o = _oracle(tr)
     o.load(tr.init_state())
@@ -89,7 +94,7 @@ def test_oracle_substep_matches_reference(scene):
     h = tr.push["f_sph"][0]
     want = tr.substep_state(1)
     err = np.abs(o.positions[:, :3].astype(np.float64) - want["positions"][:, :3]).max()
-    assert err <= 1e-4 * h, err / h
+    assert err <= 1e-5 * h, err / h
 
 
 def test_oracle_splat_matches_reference():
