@@ -43,6 +43,7 @@ PASS = {
 }
 FLAG_KEEP_DELTA = 1
 FLAG_EXACT = 2
+FLAG_REFERENCE_ORDER = 4
 
 
 class Push(ctypes.Structure):

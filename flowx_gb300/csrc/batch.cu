@@ -101,6 +101,8 @@ int flowx_batch_set_scenes(flowx_ctx *ctx, const flowx_push *pushes, int nscenes
   Ctx *c = as_ctx(ctx);
   cudaSetDevice(c->device);
   if (!pushes || nscenes < 1) return c->fail(FLOWX_ERR_ARG, "need at least one scene");
+  if (c->flags & FLOWX_FLAG_REFERENCE_ORDER)
+    return c->fail(FLOWX_ERR_ARG, "FLOWX_FLAG_REFERENCE_ORDER is for single-scene contexts");
   std::vector<SegParams> segs(nscenes);
   std::vector<long long> voxels(nscenes, 0);
   long long particles = 0, cells = 0, vox = 0;

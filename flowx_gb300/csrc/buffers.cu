@@ -451,8 +451,15 @@ int Ctx::profile_substeps(int iterations, int substeps, float *ms, int32_t *laun
       timed(K_NORMAL, 1, [&] { launch_normal_f(d, pin, d.normal_alt, exact, c->stream); });
     timed(K_PREDICT_KEY, 1, [&] { launch_predict_key(d, d.normal_alt, c->stream); });
     timed(K_SCAN_REDUCE, 3, [&] { launch_scan(d, c->stream); });
-    timed(K_SCATTER, 1, [&] { launch_scatter(d, c->stream); });
-    timed(K_CELL_SORT_SMALL, 2, [&] { launch_cell_sort(d, c->stream); });
+    if (c->flags & FLOWX_FLAG_REFERENCE_ORDER) {
+      int launched = 0;
+      timed(K_BITONIC, 0, [&] { launched = launch_reference_order(d, c->stream); });
+      launches[K_BITONIC] += launched;
+      g_launches += launched;
+    } else {
+      timed(K_SCATTER, 1, [&] { launch_scatter(d, c->stream); });
+      timed(K_CELL_SORT_SMALL, 2, [&] { launch_cell_sort(d, c->stream); });
+    }
     timed(K_PERMUTE_STEP, 1, [&] { launch_permute_step(d, d.pred_a, d.normal_alt, c->stream); });
     float4 *q_in = d.pred_a, *q_out = d.pred_b;
     for (int it = 0; it < iterations; ++it) {

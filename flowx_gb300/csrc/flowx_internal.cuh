@@ -91,6 +91,7 @@ enum KernelId {
   K_GATHER,
   K_SCATTER_IDS,
   K_VOXELIZE,
+  K_BITONIC,
   K_COUNT
 };
 
@@ -152,6 +153,10 @@ struct DeviceState {
   float4 *xv;               // per slot: velocity (pred - pos) / dt and max(rho, 1e-6) entering XSPH
   SlotQuad *quads;          // ceil(n / 4) groups: the predicted positions the next lambda or
                             // XSPH pass filters (written by permute_step, delta_apply, fill_quads)
+  unsigned long long *bitonic;  // FLOWX_FLAG_REFERENCE_ORDER: the (cell << 32 | id) array the
+                                // reference's sort network orders (bitonic_n entries)
+  uint32_t *bitonic_inv;    // per particle id: its slot before the build
+  int bitonic_n;            // next power of two >= n (the reference's sorted_count)
   const SegParams *segs;
   int32_t *slot_seg;        // per slot: its segment (read only when nseg > 1)
   int nseg;
@@ -265,6 +270,10 @@ void launch_key_only(const DeviceState &d, const float4 *pred, cudaStream_t st);
 void launch_scan(const DeviceState &d, cudaStream_t st);
 void launch_scatter(const DeviceState &d, cudaStream_t st);
 void launch_cell_sort(const DeviceState &d, cudaStream_t st);
+// FLOWX_FLAG_REFERENCE_ORDER in place of scatter + cell_sort: d.pairs from the
+// reference's bitonic network over the keys predict_key / key_only left
+// (the scan must have run); returns the number of kernels launched.
+int launch_reference_order(const DeviceState &d, cudaStream_t st);
 // writes pred_out and its copy in d.quads
 void launch_permute_step(const DeviceState &d, float4 *pred_out, const float4 *normal_in, cudaStream_t st);
 void launch_permute_all(const DeviceState &d, const float4 *pred_in, float4 *pred_out, cudaStream_t st);

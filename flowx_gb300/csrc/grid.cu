@@ -268,6 +268,119 @@ void launch_cell_sort(const DeviceState &d, cudaStream_t st)
   k_cell_sort_large<<<d.sm_count, 256, 0, st>>>(d);
 }
 
+// ---- 3'/4'. the reference's order (FLOWX_FLAG_REFERENCE_ORDER) -----------
+// The reference orders its key array with a bitonic network: sph_grid_key.glsl
+// writes entry i = (cell of particle id i, i) for i < n and (cell count, i)
+// for the padding up to S = next power of two >= n, and solver/sph.py:488-495
+// runs sph_sort.glsl for k = 2, 4, .., S and j = k/2, .., 1. Each step
+// compare-exchanges the entries i and i ^ j (i with bit j clear), swapping
+// when (key_i > key_partner) == ((i & k) == 0): by key only, so equal keys in
+// a descending block swap too and the network is unstable, but it is a fixed
+// function of the array. Running the same steps on the same array therefore
+// leaves every particle where the reference's grid build leaves it; slot k
+// then takes the particle of entry k. The pairs of one step are disjoint, so
+// the order inside a step does not matter; steps with j < kBitonicTile of a
+// k run on one tile in shared memory, the wider ones on global memory.
+constexpr int kBitonicTile = 2048;
+
+__device__ __forceinline__ void bitonic_cx(unsigned long long &x, unsigned long long &y, bool ascending)
+{
+  if (((x >> 32) > (y >> 32)) == ascending) {
+    const unsigned long long t = x;
+    x = y;
+    y = t;
+  }
+}
+
+// Entry id of the reference's key array from slot k's key (and the slot each
+// id held before this build); the padding entries after it.
+__global__ void k_bitonic_keys(DeviceState d)
+{
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= d.bitonic_n) return;
+  if (t < d.n) {
+    const uint32_t id = d.ids[t];
+    d.bitonic[id] = ((unsigned long long)d.key_tmp[t] << 32) | id;
+    d.bitonic_inv[id] = (uint32_t)t;
+  } else {
+    d.bitonic[t] = ((unsigned long long)(uint32_t)d.cells << 32) | (uint32_t)t;
+  }
+}
+
+// One step (k, j), j >= kBitonicTile: thread t takes the t-th pair.
+__global__ void k_bitonic_step(unsigned long long *__restrict__ a, int S, int k, int j)
+{
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= S / 2) return;
+  const int i = ((t & ~(j - 1)) << 1) | (t & (j - 1));
+  unsigned long long x = a[i], y = a[i | j];
+  const unsigned long long x0 = x;
+  bitonic_cx(x, y, (i & k) == 0);
+  if (x != x0) {
+    a[i] = x;
+    a[i | j] = y;
+  }
+}
+
+// Steps (k, j) for k = kmin, 2 kmin, .., kmax and j = min(k, tile) / 2, .., 1
+// on one tile of `tile` entries per block (blockDim.x = tile / 2, one pair
+// per thread and step).
+__global__ void __launch_bounds__(kBitonicTile / 2) k_bitonic_local(unsigned long long *__restrict__ a, int tile,
+                                                                    int kmin, int kmax)
+{
+  __shared__ unsigned long long sh[kBitonicTile];
+  const int base = blockIdx.x * tile;
+  for (int e = threadIdx.x; e < tile; e += blockDim.x) sh[e] = a[base + e];
+  __syncthreads();
+  const int t = threadIdx.x;
+  for (int k = kmin; k <= kmax; k <<= 1) {
+    for (int j = min(k, tile) >> 1; j > 0; j >>= 1) {
+      const int li = ((t & ~(j - 1)) << 1) | (t & (j - 1));
+      unsigned long long x = sh[li], y = sh[li | j];
+      bitonic_cx(x, y, ((base + li) & k) == 0);
+      sh[li] = x;
+      sh[li | j] = y;
+      __syncthreads();
+    }
+  }
+  for (int e = threadIdx.x; e < tile; e += blockDim.x) a[base + e] = sh[e];
+}
+
+// New slot k takes the particle of entry k: (id << 32 | its old slot), as the
+// scatter + cell sort leave d.pairs.
+__global__ void k_bitonic_pairs(DeviceState d)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= d.n) return;
+  const uint32_t id = (uint32_t)d.bitonic[k];
+  d.pairs[k] = ((unsigned long long)id << 32) | d.bitonic_inv[id];
+}
+
+int launch_reference_order(const DeviceState &d, cudaStream_t st)
+{
+  const int S = d.bitonic_n;
+  int launched = 0;
+  k_bitonic_keys<<<grid_for(S, 256), 256, 0, st>>>(d);
+  ++launched;
+  const int tile = S < kBitonicTile ? S : kBitonicTile;
+  const int tiles = S / tile;
+  k_bitonic_local<<<tiles, tile / 2, 0, st>>>(d.bitonic, tile, 2, tile);
+  ++launched;
+  for (int k = 2 * tile; k <= S; k <<= 1) {
+    for (int j = k >> 1; j >= tile; j >>= 1) {
+      k_bitonic_step<<<grid_for(S / 2, 256), 256, 0, st>>>(d.bitonic, S, k, j);
+      ++launched;
+    }
+    k_bitonic_local<<<tiles, tile / 2, 0, st>>>(d.bitonic, tile, k, k);
+    ++launched;
+  }
+  if (d.n > 0) {
+    k_bitonic_pairs<<<grid_for(d.n, 256), 256, 0, st>>>(d);
+    ++launched;
+  }
+  return launched;
+}
+
 // ---- 5. permute ---------------------------------------------------------
 // Fused substep: new slot k takes old slot s. Positions are copied, the
 // predicted position recomputed from (pos, vel, normal) exactly as predict did,

@@ -89,6 +89,26 @@ __device__ __forceinline__ float3 delta_sum_f(const SegParams &s, const DeviceSt
   return make_float3(ax, ay, az);
 }
 
+// sph_normal.glsl:56-74 for one neighbour, in the reference's arithmetic in
+// both modes: n = sum (m / rho_j) grad W_poly6 and the curvature's
+// laplacian sum. n cancels for interior particles, and sph_predict.glsl
+// divides by |n| (and |n|^2 through the curvature -lap/|n|), with the
+// speed clamp then fixing only the velocity's length: one ulp in these sums
+// moves such a particle by up to ~1e-4 of its clamped step. So the FAST
+// substep evaluates them exactly as EXACT does (same terms, same order), and
+// its normals equal EXACT's for the same inputs.
+__device__ __forceinline__ void normal_terms(const SegParams &s, float rho_j, float r2, float dx, float dy, float dz,
+                                             float &nx, float &ny, float &nz, float &lap)
+{
+  const float weight = s.mass / rho_j;
+  const float t = s.h2 - r2;
+  const float sg = s.poly6m6 * t * t;
+  nx += weight * (sg * dx);
+  ny += weight * (sg * dy);
+  nz += weight * (sg * dz);
+  lap += weight * w_visc_lap(sqrtf(r2), s.h, s.visclap);
+}
+
 // What the XSPH pass needs of slot i besides its position: the velocity
 // sph_velocity.glsl:20-23 derives from pred and the substep's starting
 // position (the same expression XSPH evaluated per neighbour), and the
@@ -158,7 +178,7 @@ __device__ __forceinline__ float3 xsph_sum_f(const SegParams &s, const DeviceSta
                                              int i, float4 q, float3 vi, VelJ &&velj, float4 *normal_out = nullptr)
 {
   const int3 base = cell_coord(s, q.x, q.y, q.z);
-  const float h = s.h, h2 = s.h2, mass = s.mass, poly6 = s.poly6;
+  const float h2 = s.h2, mass = s.mass, poly6 = s.poly6;
   const bool normals = NORMALS && s.sigma > 0.0f;
   float ax = 0.0f, ay = 0.0f, az = 0.0f;
   float nx = 0.0f, ny = 0.0f, nz = 0.0f, lap = 0.0f;
@@ -184,30 +204,16 @@ __device__ __forceinline__ float3 xsph_sum_f(const SegParams &s, const DeviceSta
       ax += (w * (vj.x - vi.x)) * wk;
       ay += (w * (vj.y - vi.y)) * wk;
       az += (w * (vj.z - vi.z)) * wk;
-      if (normals) {  // sph_normal.glsl's body, as k_normal_f
-        const float t = h2 - r2;
-        const float sg = s.poly6m6 * t * t;
-        nx += w * (sg * dx);
-        ny += w * (sg * dy);
-        nz += w * (sg * dz);
-        lap += w * w_visc_lap(sqrtf(r2), h, s.visclap);
-      }
     } else {
       const float t = __fsub_rn(h2, r2);
       const float wk = __fmul_rn(__fdividef(s.mass_poly6, rho_j), __fmul_rn(__fmul_rn(t, t), t));
       ax = __fmaf_rn(wk, __fsub_rn(vj.x, vi.x), ax);
       ay = __fmaf_rn(wk, __fsub_rn(vj.y, vi.y), ay);
       az = __fmaf_rn(wk, __fsub_rn(vj.z, vi.z), az);
-      if (normals) {
-        const float weight = __fdividef(mass, rho_j);
-        const float sg = __fmul_rn(weight, __fmul_rn(s.poly6m6, __fmul_rn(t, t)));
-        nx = __fmaf_rn(sg, dx, nx);
-        ny = __fmaf_rn(sg, dy, ny);
-        nz = __fmaf_rn(sg, dz, nz);
-        const float r = r2 > 0.0f ? __fmul_rn(r2, rsqrtf(r2)) : 0.0f;
-        lap = __fmaf_rn(__fmul_rn(weight, s.visclap), __fsub_rn(h, r), lap);
-      }
     }
+    // sph_normal.glsl's body in the reference's arithmetic in both modes
+    // (normal_terms)
+    if (normals) normal_terms(s, rho_j, r2, dx, dy, dz, nx, ny, nz, lap);
   };
   if (QUADS)
     for_each_within<EXACT>(s, d.offsets, pred, d.quads, q, h2, base, body);
@@ -255,7 +261,7 @@ __global__ void __launch_bounds__(512, 3) k_normal_f(DeviceState d, const float4
   FLOWX_SLOT_PROLOGUE
   const float4 pi = pred[i];
   const int3 base = cell_coord(s, pi.x, pi.y, pi.z);
-  const float h = s.h, h2 = s.h2, mass = s.mass, poly6m6 = s.poly6m6, vlap = s.visclap;
+  const float h2 = s.h2;
   float nx = 0.0f, ny = 0.0f, nz = 0.0f, lap = 0.0f;
   auto body = [&](int k, bool within) {
     if (k == i) return;
@@ -263,27 +269,7 @@ __global__ void __launch_bounds__(512, 3) k_normal_f(DeviceState d, const float4
     const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
     const float r2 = pair_r2<EXACT>(dx, dy, dz);
     if (!within && r2 >= h2) return;
-    const float rho_j = fmaxf(__ldg(&d.lam[k].x), 1e-6f);
-    if (EXACT) {
-      const float weight = mass / rho_j;
-      const float t = h2 - r2;
-      const float sg = poly6m6 * t * t;
-      nx += weight * (sg * dx);
-      ny += weight * (sg * dy);
-      nz += weight * (sg * dz);
-      lap += weight * w_visc_lap(sqrtf(r2), h, vlap);
-    } else {
-      const float weight = __fdividef(mass, rho_j);
-      const float t = __fsub_rn(h2, r2);
-      const float sg = __fmul_rn(weight, __fmul_rn(poly6m6, __fmul_rn(t, t)));
-      nx = __fmaf_rn(sg, dx, nx);
-      ny = __fmaf_rn(sg, dy, ny);
-      nz = __fmaf_rn(sg, dz, nz);
-      // r = sqrt(r2); coincident particles (r2 = 0, e.g. two clamped into
-      // the same box corner) have r = 0, as sqrtf gives.
-      const float r = r2 > 0.0f ? __fmul_rn(r2, rsqrtf(r2)) : 0.0f;
-      lap = __fmaf_rn(__fmul_rn(weight, vlap), __fsub_rn(h, r), lap);
-    }
+    normal_terms(s, fmaxf(__ldg(&d.lam[k].x), 1e-6f), r2, dx, dy, dz, nx, ny, nz, lap);
   };
   for_each_within<EXACT>(s, d.offsets, pred, pi, h2, base, body);
   const float mag = sqrtf(nx * nx + ny * ny + nz * nz);

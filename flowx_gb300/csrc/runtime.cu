@@ -30,7 +30,7 @@ static const char *kKernelNames[K_COUNT] = {
     "normal",        "predict_key",  "scan_reduce", "scan_top",     "scan_down",    "scatter",
     "cell_sort_small", "cell_sort_large", "permute_step", "lambda",  "delta_apply",  "xsph_finalize",
     "splat",         "predict",      "delta",       "apply_delta",  "velocity",     "xsph",
-    "finalize",      "permute_all",  "gather",      "scatter_ids",  "voxelize",
+    "finalize",      "permute_all",  "gather",      "scatter_ids",  "voxelize",     "bitonic_sort",
 };
 
 int kernel_max_threads(const void *kernel)
@@ -159,6 +159,13 @@ int Ctx::allocate()
   FLOWX_ALLOC(d_src_slot, n)
   FLOWX_ALLOC(d.row_masks, n * 9) FLOWX_ALLOC(d.row_wide, n) FLOWX_ALLOC(d.cell_lo, c) FLOWX_ALLOC(d.cell_hi, c)
   FLOWX_ALLOC(d.quads, (n + 3) / 4) FLOWX_ALLOC(d.plam, n) FLOWX_ALLOC(d.xv, n) FLOWX_ALLOC(d.slot_seg, n)
+  if (flags & FLOWX_FLAG_REFERENCE_ORDER) {
+    // solver/sph.py's sorted_count: the next power of two >= N, at least 2
+    size_t S = 2;
+    while (S < (size_t)total_particles) S <<= 1;
+    d.bitonic_n = (int)S;
+    FLOWX_ALLOC(d.bitonic, S) FLOWX_ALLOC(d.bitonic_inv, n)
+  }
 #undef FLOWX_ALLOC
   if (e != cudaSuccess) return cuda(e, "device allocation");
   d.segs = d_segs;
@@ -181,7 +188,8 @@ void Ctx::release()
   void *ptrs[] = {d.pos,    d.pos_alt, d.vel,       d.vel_alt,  d.pred_a,   d.pred_b,  d.normal,     d.normal_alt,
                   d.delta,  d.delta_alt, d.lam,     d.lam_alt,  d.stage,    d.keys,    d.ids,        d.key_tmp,
                   d.rank_tmp, d.pairs, d.pairs_tmp, d.counts,   d.offsets,  d.block_sums, d.big_cells, d.collider,
-                  d.surface, d_segs,   d_src_slot,  d_prims,  d_mesh,  d.row_masks, d.row_wide, d.cell_lo, d.cell_hi, d.quads, d.plam, d.xv, d.slot_seg};
+                  d.surface, d_segs,   d_src_slot,  d_prims,  d_mesh,  d.row_masks, d.row_wide, d.cell_lo, d.cell_hi, d.quads, d.plam, d.xv, d.slot_seg,
+                  d.bitonic, d.bitonic_inv};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (stream) cudaStreamDestroy(stream);
@@ -275,13 +283,25 @@ int Ctx::upload_segs(const std::vector<SegParams> &s, int cells)
 }
 
 // ------------------------------------------------------------ grid build
+// Cell order from the keys and the scan: the counting sort's (cell, id)
+// order, or the reference's own network (FLOWX_FLAG_REFERENCE_ORDER).
+void Ctx::issue_cell_order()
+{
+  if (flags & FLOWX_FLAG_REFERENCE_ORDER) {
+    g_launches += launch_reference_order(d, stream);
+  } else {
+    launch_scatter(d, stream);
+    launch_cell_sort(d, stream);
+    g_launches += 3;
+  }
+}
+
 void Ctx::issue_build_from_pred(const float4 *pred)
 {
   launch_key_only(d, pred, stream);
   launch_scan(d, stream);
-  launch_scatter(d, stream);
-  launch_cell_sort(d, stream);
-  g_launches += 7;
+  g_launches += 4;
+  issue_cell_order();
 }
 
 int Ctx::build_grid_generic()
@@ -327,10 +347,9 @@ int Ctx::issue_substep(int iterations, int pred_in_idx, bool normals_ready)
   }
   launch_predict_key(d, d.normal_alt, stream);
   launch_scan(d, stream);
-  launch_scatter(d, stream);
-  launch_cell_sort(d, stream);
+  issue_cell_order();
   launch_permute_step(d, d.pred_a, d.normal_alt, stream);
-  g_launches += 8;
+  g_launches += 5;
   float4 *q_in = d.pred_a, *q_out = d.pred_b;
   for (int it = 0; it < iterations; ++it) {
     launch_lambda_f(d, q_in, exact, stream);
@@ -441,6 +460,10 @@ int flowx_create(const flowx_config *config, flowx_ctx **out)
   if (config->particle_count < 0 || config->max_cells < 1 || config->max_collider_voxels < 0 ||
       config->max_surface_samples < 0) {
     g_create_error = "flowx_create: negative particle count or capacity, or max_cells < 1";
+    return FLOWX_ERR_ARG;
+  }
+  if (config->flags & ~(FLOWX_FLAG_KEEP_DELTA | FLOWX_FLAG_EXACT | FLOWX_FLAG_REFERENCE_ORDER)) {
+    g_create_error = "flowx_create: unknown bits in flags";
     return FLOWX_ERR_ARG;
   }
   if (config->particle_count > (1 << 24)) {

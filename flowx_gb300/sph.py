@@ -65,6 +65,7 @@ class Solver:
         device: int = 0,
         keep_delta: bool = False,
         exact: bool = False,
+        reference_order: bool = False,
     ):
         self.lib = _lib.load()
         self.config = config
@@ -81,7 +82,8 @@ class Solver:
         cfg.max_surface_samples = int(max_surface_samples)
         cfg.device = int(device)
         self.config_device = int(device)
-        cfg.flags = (_lib.FLAG_KEEP_DELTA if keep_delta else 0) | (_lib.FLAG_EXACT if exact else 0)
+        cfg.flags = ((_lib.FLAG_KEEP_DELTA if keep_delta else 0) | (_lib.FLAG_EXACT if exact else 0)
+                     | (_lib.FLAG_REFERENCE_ORDER if reference_order else 0))
         check(self.lib.flowx_create(ctypes.byref(cfg), ctypes.byref(self._ctx)))
         self.collider_dims = None
         self.collider_voxel = 0.0

@@ -114,6 +114,16 @@ enum {
    * (FMA, one reciprocal square root per pair), within float32 rounding. The
    * per-pass API (flowx_run_pass) is always exact. */
   FLOWX_FLAG_EXACT = 2,
+  /* Every grid build orders the particles inside each cell the way the
+   * reference's own grid build does: the bitonic compare-exchange network of
+   * sph_sort.glsl over the sph_grid_key.glsl array, driven as
+   * solver/sph.py:488-495 drives it (unstable, by cell key only). Sorted keys,
+   * cell ranges and membership are the same as without the flag; only the
+   * order inside a cell, and so the order neighbour sums visit, changes. With
+   * FLOWX_FLAG_EXACT the substep then reproduces the reference's passes
+   * in the reference's own visiting order. Costs the network's
+   * log2(S)(log2(S)+1)/2 steps per build; single-scene contexts only. */
+  FLOWX_FLAG_REFERENCE_ORDER = 4,
 };
 
 /* Sizes a context is created for (solver/sph.py:350-369 _allocate). */
@@ -427,12 +437,18 @@ int flowx_cache_read_frame_host(flowx_cache *cache, int32_t frame, float *positi
  *
  * Scratch is one static device array of the library, sized for at most
  * 65536 particles and 262144 cells; larger sizes return FLOWX_ERR_CAPACITY.
- * The first call made with a device current looks the array's address up
- * for that device: make it before any stream capture. Every call clears the
- * cell counters (the only scratch that must start at zero) itself. All calls
- * on a device share the scratch, so calls whose GPU work overlaps (different
- * streams or host threads) race: order them on one stream. The message of
- * a failure is returned by flowx_build_grid_static_error (per host thread). */
+ * The first call made with a device current is a warm-up: it looks the
+ * array's address up for that device and, with lazy module loading, is
+ * where the runtime loads the module, which reserves the array and may
+ * synchronise the device. Make it at set-up, before any stream capture;
+ * later calls allocate nothing. The address is kept for the process: do not
+ * use the library after a cudaDeviceReset. Every call clears the cell
+ * counters (the only scratch that must start at zero) itself. All calls on a
+ * device share the scratch, so calls whose GPU work overlaps race: issue
+ * them on one stream and from one host thread at a time (each call enqueues
+ * several launches; two threads' sequences on one stream can interleave).
+ * The message of a failure is returned by flowx_build_grid_static_error
+ * (per host thread). */
 int flowx_build_grid_static(const float *predicted, int32_t particle_count, const flowx_push *push, float *keys,
                             int32_t key_count, float *cell_start, float *cell_end, void *stream);
 const char *flowx_build_grid_static_error(void);

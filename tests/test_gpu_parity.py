@@ -4,8 +4,9 @@
   every pass runs on exactly the inputs the reference's pass saw (uploaded,
   including the reference's bitonic key order, so neighbour sums run in the
   reference's order), and its outputs are compared with the reference's
-  (integer work bit-exact, floats to 1e-5 of the buffer's scale) and with the
-  C oracle on the same inputs (bit-exact: same float32 operations in the same
+  (bit-exact, except delta's pow(ratio, 4.0), which the reference's harness
+  takes from glibc's powf: within 1e-6 of the buffer's scale) and with the C
+  oracle on the same inputs (bit-exact: same float32 operations in the same
   order, no FMA contraction on either side).
 * Whole fused substeps against the oracle in the (cell, id) order the CUDA
   grid build emits: bit-exact over several substeps, graph and non-graph.
@@ -18,6 +19,7 @@ from flowx_gb300 import config as C
 from flowx_gb300 import scenes
 from golden_io import TRACE_SCENES, Trace, assert_close, membership
 from oracle import oracle as O
+from rounding import assert_within_sensitivity, per_particle, ulp_neighbour
 
 pytestmark = pytest.mark.gpu
 
@@ -77,7 +79,10 @@ def test_passes_match_reference_and_oracle(scene):
                     got = s.read(b)
                     oracle_out = getattr(o, "lambda_" if b == "lambda" else b)
                     np.testing.assert_array_equal(got, oracle_out, err_msg=f"{tag}.{b} vs oracle")
-                    assert_close(f"{tag}.{b} vs reference", got, want, rel=2e-5)
+                    if name == "delta":
+                        assert_close(f"{tag}.{b} vs reference", got, want, rel=1e-6)
+                    else:
+                        np.testing.assert_array_equal(got, want, err_msg=f"{tag}.{b} vs reference")
             state.update({k: v.copy() for k, v in outs.items()})
             _load_state(s, outs)
 
@@ -139,13 +144,58 @@ def test_fused_substeps_across_calls_bit_exact(scene):
             np.testing.assert_array_equal(s.read(b), want[b], err_msg=f"{scene} {b}")
 
 
-@pytest.mark.parametrize("scene", ["dam_break", "pool_small"])
+@pytest.mark.parametrize("scene", ["dam_break", "pool_small", "pile"])
+@pytest.mark.parametrize("graph", [False, True])
+def test_reference_order_substeps_match_reference(scene, graph):
+    """The reference's own grid order (FLOWX_FLAG_REFERENCE_ORDER: its bitonic
+    network, run on the GPU) with its expressions (EXACT), from the seeded
+    state through every substep the trace holds, cohesion on: bit-exact
+    against the oracle running the same network after every substep (every
+    buffer, keys with ids), and within 1e-5 h of the reference's own passes
+    after the first (measured 6e-7 to 1.2e-6 h: delta's pow ulp is all that
+    differs). The seeded substeps amplify that ulp (a 1-ulp change of the
+    input positions moves the result by ~2e-4 h, tests/rounding.py), so the
+    distance to the reference after later substeps is reported, not bounded."""
+    tr = Trace(scene)
+    h = tr.push["f_sph"][0]
+    dt = tr.meta["dt"]
+    z = tr.z
+    o = O.Oracle(tr.push, z["init_positions"], z["init_velocities"], collider=tr.collider,
+                 iterations=tr.meta["iterations"])
+    o.build_grid(0.0, order=O.ORDER_BITONIC)
+    with _solver(tr, exact=True, reference_order=True) as s:
+        s._build_grid(0.0)
+        n = tr.meta["n"]
+        np.testing.assert_array_equal(s.read("keys", n), o.keys[:n], err_msg=f"{scene} seed grid")
+        for k in range(1, tr.meta["substeps"] + 1):
+            if graph:
+                s.step_substeps(dt, 1)
+            else:
+                s._substep(dt)
+            o.substep(dt, order=O.ORDER_BITONIC)
+            want = o.state()
+            # keys: the particles' entries (the padding entries past them hold
+            # key = cell count, which no pass reads: sph_cell_range.glsl:19-21)
+            for b in ("positions", "velocities", "predicted", "lambda", "normal", "keys", "cell_start",
+                      "cell_end"):
+                got = s.read(b, n if b == "keys" else None)
+                exp = want[b][:n] if b == "keys" else want[b]
+                np.testing.assert_array_equal(got, exp, err_msg=f"{scene} substep {k} {b} vs oracle")
+            ref = tr.substep_state(k)["positions"]
+            err = np.abs(s.read("positions")[:, :3].astype(np.float64) - ref[:, :3]).max()
+            print(f"{scene} reference order, substep {k}: {err / h:.2e} h from the reference")
+            if k == 1:
+                assert err <= 1e-5 * h, (k, err / h)
+
+
+@pytest.mark.parametrize("scene", ["dam_break", "pool_small", "pile"])
 def test_first_substep_within_tolerance_of_reference(scene):
-    """One substep from the seeded state against the reference's own passes
-    (bitonic order there, (cell, id) order here). Positions agree to 1e-4 h;
-    the oracle's own distance from the reference is the same (see
-    tests/test_oracle.py): one-ulp constant roundings amplified by the
-    cohesion term's -lap/|n|."""
+    """One substep from the seeded state, cohesion on, against the reference's
+    own passes, in the GPU's (cell, id) grid order. The visiting order inside
+    a cell differs from the reference's bitonic one, and the cohesion term
+    amplifies the resulting roundings (its normals cancel for interior
+    particles and enter the predict step through 1/|n|): both arithmetic
+    modes stay within 2e-4 h, EXACT measured at 2-9e-5 h."""
     tr = Trace(scene)
     h = tr.push["f_sph"][0]
     for exact in (True, False):
@@ -155,7 +205,8 @@ def test_first_substep_within_tolerance_of_reference(scene):
             got = s.read("positions")
         want = tr.substep_state(1)["positions"]
         err = np.abs(got[:, :3].astype(np.float64) - want[:, :3]).max()
-        assert err <= 1e-4 * h, (exact, err / h)
+        print(f"{scene} {'EXACT' if exact else 'FAST'} (cell, id) order vs reference: {err / h:.2e} h")
+        assert err <= 2e-4 * h, (exact, err / h)
 
 
 @pytest.mark.parametrize("scene", ["dam_break", "pool_small", "pile"])
@@ -205,6 +256,71 @@ def _stable_no_cohesion_scene():
     scene = scenes.dam_break()
     scene.config.surface_tension = 0.0
     return scene
+
+
+def _oracle_first_substep(tr, positions):
+    z = tr.z
+    o = O.Oracle(tr.push, positions, z["init_velocities"], collider=tr.collider, iterations=tr.meta["iterations"])
+    o.build_grid(0.0, order=O.ORDER_STABLE)
+    o.substep(tr.meta["dt"], order=O.ORDER_STABLE)
+    return o.positions.copy()
+
+
+@pytest.mark.parametrize("scene", ["dam_break", "pool_small", "pile"])
+def test_fast_first_substep_within_rounding_sensitivity_of_oracle(scene):
+    """The benchmarked arithmetic (FAST), cohesion on, one substep from the
+    seeded lattice against the oracle in the same grid order. That substep is
+    ill-conditioned (tests/rounding.py): a 1-ulp change of the input
+    positions moves the oracle's own result by up to ~2e-4 h. FAST stays
+    within a small factor of that at every quantile."""
+    tr = Trace(scene)
+    h = tr.push["f_sph"][0]
+    want = _oracle_first_substep(tr, tr.z["init_positions"])
+    noise = per_particle(_oracle_first_substep(tr, ulp_neighbour(tr.z["init_positions"])), want, h)
+    with _solver(tr, exact=False) as s:
+        s._build_grid(0.0)
+        s.step_substeps(tr.meta["dt"], 1)
+        got = s.read("positions")
+    assert_within_sensitivity(f"{scene} seeded", per_particle(got, want, h), noise)
+
+
+def test_fast_substep_within_1e5h_of_oracle_when_well_conditioned():
+    """The dam break after 8 frames (the oracle's own run, cohesion on): there
+    a 1-ulp change of the inputs moves one substep's result by at most
+    ~4e-6 h, and FAST must stay within 1e-5 h of the oracle in every
+    particle position."""
+    from flowx_gb300.sph import Solver
+
+    scene = scenes.dam_break()
+    cfg = scene.config
+    h = cfg.smoothing_radius
+    push = C.push_constant_values(cfg, scene.dt)
+    o = O.Oracle(push, scene.positions, scene.velocities, iterations=cfg.iterations)
+    o.build_grid(0.0, order=O.ORDER_STABLE)
+    for _ in range(8 * scene.substeps_per_frame):
+        o.substep(scene.dt, order=O.ORDER_STABLE)
+    st = o.state()
+
+    def oracle_one(pos):
+        q = O.Oracle(push, pos, st["velocities"], iterations=cfg.iterations)
+        q.predicted[...] = st["predicted"]
+        q.lambda_[...] = st["lambda"]
+        q.build_grid(0.0, order=O.ORDER_STABLE)
+        q.substep(scene.dt, order=O.ORDER_STABLE)
+        return q.positions.copy()
+
+    want = oracle_one(st["positions"])
+    noise = per_particle(oracle_one(ulp_neighbour(st["positions"])), want, h)
+    with Solver(cfg, st["positions"], st["velocities"]) as s:
+        s.write("predicted", st["predicted"])
+        s.write("lambda", st["lambda"])
+        s._build_grid(0.0)
+        s.step_substeps(scene.dt, 1)
+        got = s.read("positions")
+    err = per_particle(got, want, h)
+    print(f"dam break after 8 frames: FAST max {err.max():.2e} h, oracle 1-ulp sensitivity max {noise.max():.2e} h")
+    assert noise.max() <= 1e-5 / 2
+    assert err.max() <= 1e-5, err.max()
 
 
 def test_fast_substep_within_1e5h_of_oracle():
