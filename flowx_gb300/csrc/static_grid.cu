@@ -15,10 +15,16 @@
 // Host code cannot take the array's device address directly, so it is
 // fetched with cudaGetSymbolAddress once per device, during the first call
 // made with that device current; make that first call before any stream
-// capture. All calls share the one array and it keeps the last call's
-// contents: each call clears the cell counters, the only part that must
-// start at zero, and calls whose GPU work overlaps (different streams, or
-// several host threads) race on it - order them on one stream.
+// capture. That first call is a warm-up: with lazy module loading it is
+// where the runtime loads this module onto the device, which reserves the
+// array and may synchronise the device. Calls after it allocate nothing.
+// The cached address belongs to the device's primary context: after a
+// cudaDeviceReset the library must not be used again in the process.
+// All calls share the one array and it keeps the last call's contents: each
+// call clears the cell counters, the only part that must start at zero, and
+// calls whose GPU work overlaps race on it. So issue them on one stream and
+// from one host thread at a time (each call enqueues several launches, and
+// two threads' sequences on one stream can interleave).
 #include <mutex>
 #include <string>
 
@@ -194,7 +200,9 @@ int flowx_build_grid_static(const float *predicted, int32_t particle_count, cons
   launch_scan(d, st);
   launch_scatter(d, st);
   launch_cell_sort(d, st);
-  launched += 3 + (particle_count > 0 ? 1 : 0) + 2;
+  // scan: 3 launches; scatter and the per-slot cell ranking: one each when
+  // there are particles; the large-cell sorter: always one
+  launched += 3 + (particle_count > 0 ? 2 : 0) + 1;
   if (key_count > 0) {
     k_write_keys<<<(key_count + 255) / 256, 256, 0, st>>>(d.pairs, d.key_tmp, particle_count, key_count, (int)cells,
                                                           reinterpret_cast<float4 *>(keys));

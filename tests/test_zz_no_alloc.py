@@ -107,6 +107,41 @@ def test_static_grid_small_scene_and_reuse_after_larger_call():
             _assert_same(_static_build(pts, push, cfg.sorted_count, cfg.cell_count), want)
 
 
+def test_static_grid_allocates_nothing_after_the_first_call():
+    """The first call on a device is a warm-up (the runtime may load the
+    library's module there, reserving the static scratch); the calls after
+    it leave the device's free memory unchanged. The caller's buffers are
+    made once, before the calls."""
+    import torch
+
+    from flowx_gb300.sph import Solver
+
+    lib = _lib.load()
+    sc = scenes.dam_break()
+    cfg = sc.config
+    with Solver(cfg, sc.positions, sc.velocities) as s:
+        push = s.push(0.0)
+    pred = torch.from_numpy(np.ascontiguousarray(sc.positions, np.float32)).to("cuda:0")
+    keys = torch.zeros((cfg.sorted_count, 4), dtype=torch.float32, device="cuda:0")
+    start = torch.zeros(cfg.cell_count, dtype=torch.float32, device="cuda:0")
+    end = torch.zeros(cfg.cell_count, dtype=torch.float32, device="cuda:0")
+    stream = ctypes.c_void_p(torch.cuda.current_stream(0).cuda_stream)
+
+    def call():
+        rc = lib.flowx_build_grid_static(pred.data_ptr(), sc.n, ctypes.byref(push), keys.data_ptr(),
+                                         cfg.sorted_count, start.data_ptr(), end.data_ptr(), stream)
+        assert rc == _lib.FLOWX_OK, lib.flowx_build_grid_static_error().decode()
+        torch.cuda.synchronize(0)
+        return torch.cuda.mem_get_info(0)[0]
+
+    before = call()  # warm-up; free memory after it
+    free = [call() for _ in range(3)]
+    assert all(f == before for f in free), (before, free)
+    first = (keys.cpu().numpy(), start.cpu().numpy(), end.cpu().numpy())
+    call()
+    _assert_same((keys.cpu().numpy(), start.cpu().numpy(), end.cpu().numpy()), first)
+
+
 def test_static_grid_rejects_sizes_beyond_the_static_scratch():
     import torch
 
