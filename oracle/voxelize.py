@@ -16,9 +16,12 @@ when the column point lies inside the triangle's xy projection (edge
 functions evaluated from the lexicographically smaller endpoint, so that two
 triangles sharing an edge see exactly opposite values, and points exactly on
 an edge or vertex decided as if displaced by (eps, eps^2)), and a centre
-counts a crossing strictly above it. Parity against Blender's ray casts is
-unpinned; the restatement is pinned instead against analytic shapes in
-tests/test_voxelize_oracle.py, and the GPU voxeliser against it bit for bit.
+counts a crossing strictly above it. It is pinned against the reference's own
+voxeliser code run outside Blender, with only the BVH ray cast a stand-in
+(tests/golden/make_voxel_golden.py, tests/test_voxelize_reference.py: equal
+on every case but voxel centres lying exactly on a mesh face), and against
+analytic shapes (tests/test_voxelize_oracle.py); the GPU voxeliser is
+checked against it bit for bit.
 
 Only the tests use this module.
 """

@@ -1,13 +1,15 @@
 """GPU mesh voxeliser (flowx_voxelize_meshes) against its CPU restatement
-(oracle/voxelize.py, itself checked against analytic shapes): identical
-occupancy grids for boxes, rotated and scaled meshes, a lattice-aligned
-octahedron, a UV sphere, a torus and unions, up to a 100^3 grid; bad triangle
-indices are rejected before anything runs."""
+(oracle/voxelize.py, itself checked against analytic shapes and against the
+reference's own voxeliser code): identical occupancy grids for boxes, rotated
+and scaled meshes, a lattice-aligned octahedron, a UV sphere, a torus and
+unions, up to a 100^3 grid; and against the reference's grids directly; bad
+triangle indices are rejected before anything runs."""
 
 import numpy as np
 import pytest
 
 import mesh_shapes as S
+import test_voxelize_reference as R
 from oracle import voxelize as V
 
 pytestmark = pytest.mark.gpu
@@ -59,6 +61,17 @@ def test_gpu_equals_oracle(name):
         again = _gpu_grid(s, meshes, dims, voxel, origin)  # scratch reused
     np.testing.assert_array_equal(got, want)
     np.testing.assert_array_equal(again, want)
+
+
+@pytest.mark.parametrize("name", sorted(R.CASES))
+def test_gpu_matches_reference_voxeliser(name):
+    """Against the grids of the reference's own voxeliser code
+    (tests/test_voxelize_reference.py): equal voxel for voxel, except the
+    listed centres that lie exactly on the lattice octahedron's faces."""
+    meshes, dims, voxel, origin, _ = R.CASES[name]
+    with _solver(int(np.prod(dims))) as s:
+        got = _gpu_grid(s, meshes, dims, voxel, origin)
+    R.check_against_reference(name, got)
 
 
 def test_bad_triangle_index_is_rejected():
