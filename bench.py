@@ -301,21 +301,48 @@ def _mesh_voxelizer_metrics(scene, reps=5):
             "timing": "wall clock of Solver.voxelize_meshes (upload, two kernels), synchronised"}
 
 
-def _batched_metrics(substeps=20, warmup=3):
-    """The 64-scene batched workload (particle counts log-uniform in
-    [2e3, 2e5]): one context stepping all scenes per launch, against the same
-    scenes stepped one after another, each in its own context with its own
-    CUDA graph. Both timed with CUDA events over ``substeps`` substeps after
-    ``warmup`` untimed ones."""
+def kernel_source_digest() -> str:
+    """sha256 over the library's kernel sources (flowx_gb300/csrc, sorted by
+    name): the build an ncu capture was taken of."""
+    import hashlib
+
+    h = hashlib.sha256()
+    src = os.path.join(ROOT, "flowx_gb300", "csrc")
+    for name in sorted(os.listdir(src)):
+        if name.endswith((".cu", ".cuh", ".h")):
+            h.update(name.encode())
+            with open(os.path.join(src, name), "rb") as f:
+                h.update(f.read())
+    return h.hexdigest()
+
+
+def _capture_of_this_build():
+    """Per-launch DRAM bytes and warp instructions of the dominant kernels
+    from the committed summary of an ncu capture (profiles/traffic.json),
+    used only when that capture was taken of exactly these kernel sources;
+    otherwise None (the figures are then reported as null)."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        rec = json.load(f)
+    if rec.get("kernel_source_sha256") != kernel_source_digest():
+        return None
+    rec["source"] = f"profiles/traffic.json ({rec.get('capture', 'ncu capture')})"
+    return rec
+
+
+BATCH_BUCKETS = ((2000, 20000), (20000, 200001))
+
+
+def _time_batch(scenes_, substeps, warmup):
+    """Device time of ``substeps`` batched substeps (one context, one launch
+    per pass for all scenes, autotuned), CUDA events on its stream."""
     import torch
 
-    from flowx_gb300 import scenes
     from flowx_gb300.batch import Batch
-    from flowx_gb300.sph import Solver
 
-    sc = scenes.batched_scenes()
-    total = sum(s.n for s in sc)
-    with Batch(sc) as b:
+    with Batch(scenes_) as b:
         b.build_grid()
         tuned = b.autotune(4)
         for _ in range(warmup):
@@ -328,25 +355,70 @@ def _batched_metrics(substeps=20, warmup=3):
             b.step(4, 1)
         e1.record(stream)
         e1.synchronize()
-        batched_ms = e0.elapsed_time(e1)
-    solvers = [Solver(s.config, s.positions, s.velocities, collider=s.collider_grid(0), collider_voxel=s.collider_voxel)
-               for s in sc]
-    for s, sol in zip(sc, solvers):
-        sol._build_grid(0.0)
-        for _ in range(warmup):
-            sol.step_substeps(s.dt, 1)
-        sol.synchronize()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(substeps):
-        for s, sol in zip(sc, solvers):
-            sol.step_substeps(s.dt, 1)
-    for sol in solvers:
-        sol.synchronize()
-    seq_s = time.perf_counter() - t0
-    for sol in solvers:
-        sol.close()
-    batched = total * substeps / (batched_ms / 1e3)
+        return e0.elapsed_time(e1) / 1e3, tuned
+
+
+def _time_per_scene(scenes_, substeps, warmup, sequential):
+    """The plain path per scene: each scene its own context and one-substep
+    CUDA graph. sequential: scene after scene, each substep finished
+    (synchronised) before the next scene's starts, so one scene runs at a
+    time. Otherwise every scene's launch is issued at once and the scenes run
+    concurrently on their own streams. Wall clock, synchronised at both
+    ends."""
+    import torch
+
+    from flowx_gb300.sph import Solver
+
+    solvers = [Solver(s.config, s.positions, s.velocities, collider=s.collider_grid(0),
+                      collider_voxel=s.collider_voxel) for s in scenes_]
+    try:
+        for s, sol in zip(scenes_, solvers):
+            sol._build_grid(0.0)
+            for _ in range(warmup):
+                sol.step_substeps(s.dt, 1)
+            sol.synchronize()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(substeps):
+            for s, sol in zip(scenes_, solvers):
+                sol.step_substeps(s.dt, 1)
+                if sequential:
+                    sol.synchronize()
+        for sol in solvers:
+            sol.synchronize()
+        return time.perf_counter() - t0
+    finally:
+        for sol in solvers:
+            sol.close()
+
+
+def _batched_metrics(substeps=20, warmup=3):
+    """The 64-scene batched workload (particle counts log-uniform in
+    [2e3, 2e5], seed 3): one context stepping all scenes per launch, against
+    the plain path run per scene sequentially (one scene at a time), over
+    ``substeps`` substeps after ``warmup`` untimed ones. Also: the per-scene
+    contexts issued at once on their own streams (concurrent, not a
+    sequential run), and the batch against the sequential path per
+    scene-size bucket."""
+    from flowx_gb300 import scenes
+
+    sc = scenes.batched_scenes()
+    total = sum(s.n for s in sc)
+    batched_s, tuned = _time_batch(sc, substeps, warmup)
+    seq_s = _time_per_scene(sc, substeps, warmup, sequential=True)
+    conc_s = _time_per_scene(sc, substeps, warmup, sequential=False)
+    buckets = []
+    for lo, hi in BATCH_BUCKETS:
+        part = [s for s in sc if lo <= s.n < hi]
+        if not part:
+            continue
+        n = sum(s.n for s in part)
+        b_s, _ = _time_batch(part, substeps, warmup)
+        q_s = _time_per_scene(part, substeps, warmup, sequential=True)
+        buckets.append({"particles_range": [lo, hi - 1], "scenes": len(part), "particles": n,
+                        "batched_value": n * substeps / b_s, "sequential_value": n * substeps / q_s,
+                        "speedup_vs_sequential": q_s / b_s})
+    batched = total * substeps / batched_s
     sequential = total * substeps / seq_s
     return {
         "scenes": len(sc),
@@ -356,10 +428,18 @@ def _batched_metrics(substeps=20, warmup=3):
         "sequential_value": sequential,
         "unit": UNIT,
         "speedup_vs_sequential": batched / sequential,
-        "ms_per_substep": batched_ms / substeps,
+        "target_speedup": 3.0,
+        "ms_per_substep": batched_s * 1e3 / substeps,
+        "sequential_ms_per_substep": seq_s * 1e3 / substeps,
+        "concurrent_streams_value": total * substeps / conc_s,
+        "speedup_vs_concurrent_streams": conc_s / batched_s,
+        "buckets": buckets,
         "autotuned_blocks": tuned,
-        "sequential": "each scene its own context and one-substep CUDA graph, issued one after another from one "
-                      "host thread (wall clock, synchronised at both ends)",
+        "sequential": "the plain path per scene, sequentially: each scene its own context and one-substep CUDA "
+                      "graph, each substep synchronised before the next scene's (wall clock)",
+        "concurrent_streams": "the same contexts, every scene's substep issued before any is waited for (the "
+                              "scenes' streams overlap on the GPU; wall clock)",
+        "timing": "batched: CUDA events on the batch's stream",
     }
 
 
@@ -458,20 +538,30 @@ def run_reference(args):
     scene = _workload(args)
     c = scene.config
     ic = C.collider_binding(scene.collider_dims, scene.collider_voxel)
-    o = O.Oracle(C.push_constant_values(c, scene.dt, ic), scene.positions, scene.velocities,
-                 collider=scene.collider_grid(0), iterations=c.iterations)
-    o.build_grid(0.0, order=O.ORDER_STABLE)
     cores = O.max_threads()
-    for _ in range(args.warmup):
-        o.substep(scene.dt, order=O.ORDER_STABLE)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        o.substep(scene.dt, order=O.ORDER_STABLE)
-    elapsed = time.perf_counter() - t0
+
+    def timed(order, steps, warmup):
+        o = O.Oracle(C.push_constant_values(c, scene.dt, ic), scene.positions, scene.velocities,
+                     collider=scene.collider_grid(0), iterations=c.iterations)
+        o.build_grid(0.0, order=order)
+        for _ in range(warmup):
+            o.substep(scene.dt, order=order)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            o.substep(scene.dt, order=order)
+        return time.perf_counter() - t0
+
+    # value: the reference's own grid build, the bitonic network of
+    # sph_sort.glsl driven as solver/sph.py:488-495 does (log2(S)(log2(S)+1)/2
+    # compare-exchange passes over the padded key array); beside it the same
+    # passes with the (cell, id) counting-sort order the GPU path emits.
+    elapsed = timed(O.ORDER_BITONIC, args.steps, args.warmup)
+    stable_steps = max(1, min(args.steps, 2))
+    stable_s = timed(O.ORDER_STABLE, stable_steps, 1)
     value = scene.n * args.steps / elapsed
-    sample = (f"each step is one substep of the full {scene.n}-particle workload (oracle C restatement of the "
-              f"reference passes, OpenMP {cores} threads); the reference's own GLSL passes need a graphics "
-              f"stack, unavailable on this box")
+    sample = (f"each step is one substep of the full {scene.n}-particle workload: the oracle C restatement of "
+              f"the reference passes with the reference's bitonic key sort, OpenMP {cores} threads; the "
+              f"reference's own GLSL passes need a graphics stack, unavailable on this box")
     line = {
         "impl": "reference",
         "metric": METRIC,
@@ -489,6 +579,9 @@ def run_reference(args):
         "config": _workload_config(scene, args, {"step": "one substep (host CPU)"}),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "grid_order": "bitonic (the reference's sort network; value)",
+        "stable_order": {"value": scene.n * stable_steps / stable_s, "unit": UNIT, "steps": stable_steps,
+                         "note": "same passes, grid sorted into (cell, id) order by a counting sort"},
         "oracle_build": oracle_build_ok,
     }
     print(json.dumps(line))
@@ -573,15 +666,9 @@ def run_flowx(args):
     dom_bytes = BYTES_PER_PARTICLE.get(dominant, 0) * scene.n
     dom_ms = prof[dominant][0] / prof[dominant][1]
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
-    traffic = None
-    traffic_path = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(traffic_path):
-        with open(traffic_path) as f:
-            traffic = json.load(f).get("bytes_per_launch", {}).get(dominant)
-    warp_inst = None
-    if os.path.exists(traffic_path):
-        with open(traffic_path) as f:
-            warp_inst = json.load(f).get("warp_instructions_per_launch", {}).get(dominant)
+    capture = _capture_of_this_build()
+    traffic = capture.get("bytes_per_launch", {}).get(dominant) if capture else None
+    warp_inst = capture.get("warp_instructions_per_launch", {}).get(dominant) if capture else None
     roofline = {
         "bound": "hbm",
         "kernel": dominant,
@@ -591,6 +678,8 @@ def run_flowx(args):
         "unit": "GB/s",
         "frac": achieved / peak,
         "traffic": traffic,
+        "traffic_source": (capture["source"] if capture else "null: no ncu capture of this build's kernel sources "
+                           "is committed"),
         "algorithmic_bytes_per_launch": dom_bytes,
         "ms_per_launch": dom_ms,
     }
