@@ -44,6 +44,9 @@ PASS = {
 FLAG_KEEP_DELTA = 1
 FLAG_EXACT = 2
 FLAG_REFERENCE_ORDER = 4
+FLAG_WARP_PASSES = 8
+FLAG_THREAD_PASSES = 16
+WARP_PASSES_MAX_PARTICLES = 25000
 
 
 class Push(ctypes.Structure):

@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libflowx.so")
-SOURCES = ["grid.cu", "pbf.cu", "runtime.cu", "buffers.cu", "batch.cu", "static_grid.cu", "adjoint.cu", "mc.cu", "cache.cu", "voxel.cu"]
+SOURCES = ["grid.cu", "pbf.cu", "pbf_warp.cu", "runtime.cu", "buffers.cu", "batch.cu", "static_grid.cu", "adjoint.cu", "mc.cu", "cache.cu", "voxel.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 

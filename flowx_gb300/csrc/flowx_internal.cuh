@@ -160,6 +160,7 @@ struct DeviceState {
   const SegParams *segs;
   int32_t *slot_seg;        // per slot: its segment (read only when nseg > 1)
   int nseg;
+  int warp_passes;          // neighbour passes one warp per particle (pbf_warp.cu), else one thread
   int n;                    // total particles
   int cells;                // total cells
   int sm_count;             // multiprocessors of the context's device
@@ -300,6 +301,15 @@ void launch_xsph_inputs(const DeviceState &d, const float4 *pred, bool exact, cu
 void launch_xsph_finalize_f(const DeviceState &d, const float4 *pred, float4 *pos_out, bool keep_delta, bool exact,
                             bool normals, cudaStream_t st);
 void launch_normal_f(const DeviceState &d, const float4 *pred, float4 *out, bool exact, cudaStream_t st);
+// The same passes one warp per particle (pbf_warp.cu), bit-identical to the
+// thread-per-particle kernels; the launch_*_f wrappers call them when
+// d.warp_passes is set.
+void launch_lambda_w(const DeviceState &d, const float4 *pred, bool exact, cudaStream_t st);
+void launch_delta_apply_w(const DeviceState &d, const float4 *pred_in, float4 *pred_out, bool exact, bool last,
+                          cudaStream_t st);
+void launch_xsph_finalize_w(const DeviceState &d, const float4 *pred, float4 *pos_out, bool keep_delta, bool exact,
+                            bool normals, cudaStream_t st);
+void launch_normal_w(const DeviceState &d, const float4 *pred, float4 *out, bool exact, cudaStream_t st);
 // The splat of one segment (cells [cell_begin, cell_begin + cell_count)):
 // refreshes those cells' position bounds, then gathers every sample.
 void launch_splat_segment(const DeviceState &d, int seg, int cell_begin, int cell_count, const float *surface_lo,

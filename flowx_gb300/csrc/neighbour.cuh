@@ -334,6 +334,32 @@ __device__ __forceinline__ void for_each_within_recorded(const SegParams &s, con
   visit_row_masks(s, off, base, mine, stride, f);
 }
 
+// sph_velocity.glsl:20-23 for one slot.
+__device__ __forceinline__ float3 slot_velocity(const float4 &q, const float4 &p, float dtc)
+{
+  return make_float3((q.x - p.x) / dtc, (q.y - p.y) / dtc, (q.z - p.z) / dtc);
+}
+
+// What the XSPH pass needs of slot i besides its position: the velocity
+// sph_velocity.glsl:20-23 derives from pred and the substep's starting
+// position (the same expression XSPH evaluated per neighbour), and the
+// density floor sph_xsph.glsl applies.
+template <bool EXACT>
+__device__ __forceinline__ float4 xsph_input(const SegParams &s, const DeviceState &d, int i, float4 q)
+{
+  const float4 p0 = d.pos_alt[i];
+  const float dtc = s.dtc;
+  float3 v;
+  if (EXACT) {
+    v = slot_velocity(q, p0, dtc);
+  } else {
+    const float inv_dtc = 1.0f / dtc;
+    v = make_float3(__fmul_rn(__fsub_rn(q.x, p0.x), inv_dtc), __fmul_rn(__fsub_rn(q.y, p0.y), inv_dtc),
+                    __fmul_rn(__fsub_rn(q.z, p0.z), inv_dtc));
+  }
+  return make_float4(v.x, v.y, v.z, fmaxf(d.lam[i].x, 1e-6f));
+}
+
 // ---- pass bodies ----------------------------------------------------------
 // EXACT: the reference's expressions, operation for operation (bit-identical
 // to the oracle). FAST: the same quantities re-associated for throughput (FMA,

@@ -27,12 +27,6 @@ static inline unsigned grid_for(long long n, int b) { return (unsigned)((n + b -
   if (i >= d.n) return;                                \
   const SegParams &s = d.segs[slot_segment(d, i)];
 
-// sph_velocity.glsl:20-23 for one slot.
-__device__ __forceinline__ float3 slot_velocity(const float4 &q, const float4 &p, float dtc)
-{
-  return make_float3((q.x - p.x) / dtc, (q.y - p.y) / dtc, (q.z - p.z) / dtc);
-}
-
 // ---- neighbour passes -------------------------------------------------------
 
 // Register bounds of the neighbour kernels below, each measured on the
@@ -89,44 +83,33 @@ __device__ __forceinline__ float3 delta_sum_f(const SegParams &s, const DeviceSt
   return make_float3(ax, ay, az);
 }
 
-// sph_normal.glsl:56-74 for one neighbour, in the reference's arithmetic in
-// both modes: n = sum (m / rho_j) grad W_poly6 and the curvature's
-// laplacian sum. n cancels for interior particles, and sph_predict.glsl
-// divides by |n| (and |n|^2 through the curvature -lap/|n|), with the
-// speed clamp then fixing only the velocity's length: one ulp in these sums
-// moves such a particle by up to ~1e-4 of its clamped step. So the FAST
-// substep evaluates them exactly as EXACT does (same terms, same order), and
-// its normals equal EXACT's for the same inputs.
+// sph_normal.glsl:56-74 for one neighbour: n = sum (m / rho_j) grad W_poly6
+// and the curvature's laplacian sum. EXACT: the reference's operations; FAST:
+// re-associated (FMA, one reciprocal square root).
+template <bool EXACT>
 __device__ __forceinline__ void normal_terms(const SegParams &s, float rho_j, float r2, float dx, float dy, float dz,
                                              float &nx, float &ny, float &nz, float &lap)
 {
-  const float weight = s.mass / rho_j;
-  const float t = s.h2 - r2;
-  const float sg = s.poly6m6 * t * t;
-  nx += weight * (sg * dx);
-  ny += weight * (sg * dy);
-  nz += weight * (sg * dz);
-  lap += weight * w_visc_lap(sqrtf(r2), s.h, s.visclap);
-}
-
-// What the XSPH pass needs of slot i besides its position: the velocity
-// sph_velocity.glsl:20-23 derives from pred and the substep's starting
-// position (the same expression XSPH evaluated per neighbour), and the
-// density floor sph_xsph.glsl applies.
-template <bool EXACT>
-__device__ __forceinline__ float4 xsph_input(const SegParams &s, const DeviceState &d, int i, float4 q)
-{
-  const float4 p0 = d.pos_alt[i];
-  const float dtc = s.dtc;
-  float3 v;
   if (EXACT) {
-    v = slot_velocity(q, p0, dtc);
+    const float weight = s.mass / rho_j;
+    const float t = s.h2 - r2;
+    const float sg = s.poly6m6 * t * t;
+    nx += weight * (sg * dx);
+    ny += weight * (sg * dy);
+    nz += weight * (sg * dz);
+    lap += weight * w_visc_lap(sqrtf(r2), s.h, s.visclap);
   } else {
-    const float inv_dtc = 1.0f / dtc;
-    v = make_float3(__fmul_rn(__fsub_rn(q.x, p0.x), inv_dtc), __fmul_rn(__fsub_rn(q.y, p0.y), inv_dtc),
-                    __fmul_rn(__fsub_rn(q.z, p0.z), inv_dtc));
+    const float weight = __fdividef(s.mass, rho_j);
+    const float t = __fsub_rn(s.h2, r2);
+    const float sg = __fmul_rn(weight, __fmul_rn(s.poly6m6, __fmul_rn(t, t)));
+    nx = __fmaf_rn(sg, dx, nx);
+    ny = __fmaf_rn(sg, dy, ny);
+    nz = __fmaf_rn(sg, dz, nz);
+    // r = sqrt(r2); coincident particles (r2 = 0, e.g. two clamped into the
+    // same box corner) have r = 0, as sqrtf gives.
+    const float r = r2 > 0.0f ? __fmul_rn(r2, rsqrtf(r2)) : 0.0f;
+    lap = __fmaf_rn(__fmul_rn(weight, s.visclap), __fsub_rn(s.h, r), lap);
   }
-  return make_float4(v.x, v.y, v.z, fmaxf(d.lam[i].x, 1e-6f));
 }
 
 // sph_delta.glsl + sph_apply_delta.glsl: pred_out = pred_in + sum / rho0.
@@ -211,9 +194,7 @@ __device__ __forceinline__ float3 xsph_sum_f(const SegParams &s, const DeviceSta
       ay = __fmaf_rn(wk, __fsub_rn(vj.y, vi.y), ay);
       az = __fmaf_rn(wk, __fsub_rn(vj.z, vi.z), az);
     }
-    // sph_normal.glsl's body in the reference's arithmetic in both modes
-    // (normal_terms)
-    if (normals) normal_terms(s, rho_j, r2, dx, dy, dz, nx, ny, nz, lap);
+    if (normals) normal_terms<EXACT>(s, rho_j, r2, dx, dy, dz, nx, ny, nz, lap);  // sph_normal.glsl's body
   };
   if (QUADS)
     for_each_within<EXACT>(s, d.offsets, pred, d.quads, q, h2, base, body);
@@ -269,7 +250,7 @@ __global__ void __launch_bounds__(512, 3) k_normal_f(DeviceState d, const float4
     const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
     const float r2 = pair_r2<EXACT>(dx, dy, dz);
     if (!within && r2 >= h2) return;
-    normal_terms(s, fmaxf(__ldg(&d.lam[k].x), 1e-6f), r2, dx, dy, dz, nx, ny, nz, lap);
+    normal_terms<EXACT>(s, fmaxf(__ldg(&d.lam[k].x), 1e-6f), r2, dx, dy, dz, nx, ny, nz, lap);
   };
   for_each_within<EXACT>(s, d.offsets, pred, pi, h2, base, body);
   const float mag = sqrtf(nx * nx + ny * ny + nz * nz);
@@ -279,6 +260,7 @@ __global__ void __launch_bounds__(512, 3) k_normal_f(DeviceState d, const float4
 
 void launch_lambda_f(const DeviceState &d, const float4 *pred, bool exact, cudaStream_t st)
 {
+  if (d.warp_passes) return launch_lambda_w(d, pred, exact, st);
   const int b = FLOWX_BLOCK(d, K_LAMBDA, 128, exact ? (const void *)k_lambda_f<true> : (const void *)k_lambda_f<false>);
   if (d.n <= 0) return;
   if (exact) k_lambda_f<true><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred);
@@ -287,6 +269,7 @@ void launch_lambda_f(const DeviceState &d, const float4 *pred, bool exact, cudaS
 void launch_delta_apply_f(const DeviceState &d, const float4 *pred_in, float4 *pred_out, bool exact, bool last,
                           cudaStream_t st)
 {
+  if (d.warp_passes) return launch_delta_apply_w(d, pred_in, pred_out, exact, last, st);
   const int b = FLOWX_BLOCK(d, K_DELTA_APPLY, 128,
                             exact ? (const void *)k_delta_apply_f<true> : (const void *)k_delta_apply_f<false>);
   if (d.n <= 0) return;
@@ -303,6 +286,7 @@ void launch_xsph_inputs(const DeviceState &d, const float4 *pred, bool exact, cu
 void launch_xsph_finalize_f(const DeviceState &d, const float4 *pred, float4 *pos_out, bool keep_delta, bool exact,
                             bool normals, cudaStream_t st)
 {
+  if (d.warp_passes) return launch_xsph_finalize_w(d, pred, pos_out, keep_delta, exact, normals, st);
   const void *fn = exact ? (normals ? (const void *)k_xsph_finalize_f<true, true>
                                     : (const void *)k_xsph_finalize_f<true, false>)
                          : (normals ? (const void *)k_xsph_finalize_f<false, true>
@@ -318,6 +302,7 @@ void launch_xsph_finalize_f(const DeviceState &d, const float4 *pred, float4 *po
 }
 void launch_normal_f(const DeviceState &d, const float4 *pred, float4 *out, bool exact, cudaStream_t st)
 {
+  if (d.warp_passes) return launch_normal_w(d, pred, out, exact, st);
   const int b = FLOWX_BLOCK(d, K_NORMAL, 128, exact ? (const void *)k_normal_f<true> : (const void *)k_normal_f<false>);
   if (d.n <= 0) return;
   if (exact) k_normal_f<true><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred, out);

@@ -172,6 +172,9 @@ int Ctx::allocate()
   d.nseg = (int)segs.size();
   d.n = total_particles;
   d.cells = 0;
+  d.warp_passes = (flags & FLOWX_FLAG_WARP_PASSES) ? 1
+                  : (flags & FLOWX_FLAG_THREAD_PASSES) ? 0
+                  : (total_particles <= FLOWX_WARP_PASSES_MAX_PARTICLES ? 1 : 0);
   // ids start as the identity: slot k holds particle k.
   std::vector<uint32_t> ident(n);
   for (size_t k = 0; k < n; ++k) ident[k] = (uint32_t)k;
@@ -462,8 +465,13 @@ int flowx_create(const flowx_config *config, flowx_ctx **out)
     g_create_error = "flowx_create: negative particle count or capacity, or max_cells < 1";
     return FLOWX_ERR_ARG;
   }
-  if (config->flags & ~(FLOWX_FLAG_KEEP_DELTA | FLOWX_FLAG_EXACT | FLOWX_FLAG_REFERENCE_ORDER)) {
+  if (config->flags & ~(FLOWX_FLAG_KEEP_DELTA | FLOWX_FLAG_EXACT | FLOWX_FLAG_REFERENCE_ORDER |
+                        FLOWX_FLAG_WARP_PASSES | FLOWX_FLAG_THREAD_PASSES)) {
     g_create_error = "flowx_create: unknown bits in flags";
+    return FLOWX_ERR_ARG;
+  }
+  if ((config->flags & FLOWX_FLAG_WARP_PASSES) && (config->flags & FLOWX_FLAG_THREAD_PASSES)) {
+    g_create_error = "flowx_create: FLOWX_FLAG_WARP_PASSES and FLOWX_FLAG_THREAD_PASSES exclude each other";
     return FLOWX_ERR_ARG;
   }
   if (config->particle_count > (1 << 24)) {

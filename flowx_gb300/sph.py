@@ -49,7 +49,15 @@ def _f4(arr, n):
 
 
 class Solver:
-    """One domain's PBF state on the GPU."""
+    """One domain's PBF state on the GPU.
+
+    exact: the reference's float expressions operation for operation
+    (FLOWX_FLAG_EXACT); reference_order: every grid build orders each cell
+    the way the reference's bitonic network does (FLOWX_FLAG_REFERENCE_ORDER);
+    passes: "warp" or "thread" per particle for the neighbour passes, or
+    "auto" (warp up to WARP_PASSES_MAX_PARTICLES particles). Results do not
+    depend on `passes`.
+    """
 
     def __init__(
         self,
@@ -66,6 +74,7 @@ class Solver:
         keep_delta: bool = False,
         exact: bool = False,
         reference_order: bool = False,
+        passes: str = "auto",
     ):
         self.lib = _lib.load()
         self.config = config
@@ -82,8 +91,11 @@ class Solver:
         cfg.max_surface_samples = int(max_surface_samples)
         cfg.device = int(device)
         self.config_device = int(device)
+        if passes not in ("auto", "warp", "thread"):
+            raise ValueError(f"passes must be 'auto', 'warp' or 'thread', not {passes!r}")
         cfg.flags = ((_lib.FLAG_KEEP_DELTA if keep_delta else 0) | (_lib.FLAG_EXACT if exact else 0)
-                     | (_lib.FLAG_REFERENCE_ORDER if reference_order else 0))
+                     | (_lib.FLAG_REFERENCE_ORDER if reference_order else 0)
+                     | {"auto": 0, "warp": _lib.FLAG_WARP_PASSES, "thread": _lib.FLAG_THREAD_PASSES}[passes])
         check(self.lib.flowx_create(ctypes.byref(cfg), ctypes.byref(self._ctx)))
         self.collider_dims = None
         self.collider_voxel = 0.0

