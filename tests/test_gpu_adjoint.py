@@ -202,9 +202,9 @@ def test_adjoint_matches_float64_adjoint_along_trajectory(name, substeps):
 def test_rollout_autograd_function_and_inverse_problem():
     """The full 20,000-particle, 30-substep problem gives a finite gradient of
     the control grid; over a 3-substep rollout, where the loss is smooth on
-    the optimiser's scale, Adam lowers it steadily. (Over 30 substeps the
-    gradient is exact but grows about 3.6x per substep, so Adam's steps leave
-    the region it describes.)"""
+    the optimiser's scale, plain Adam lowers it steadily. (Over 30 substeps the
+    gradient is exact but grows about 3.6x per substep, so plain Adam's steps
+    leave the region it describes; see the continuation test below.)"""
     import torch
 
     from flowx_gb300.adjoint import InverseProblem
@@ -215,7 +215,21 @@ def test_rollout_autograd_function_and_inverse_problem():
     loss.backward()
     assert torch.isfinite(loss) and torch.isfinite(control.grad).all() and float(control.grad.abs().sum()) > 0.0
     short = InverseProblem(scenes.inverse_problem(n_block=(20, 10, 10)), substeps=3)
-    losses, _ = short.optimise(steps=10, lr=0.05)
+    losses, _ = short.optimise(steps=10, lr=0.05, method="adam")
     assert np.isfinite(losses).all()
     assert all(b < a for a, b in zip(losses, losses[1:]))
     assert losses[-1] < 0.7 * losses[0]
+
+
+def test_inverse_problem_continuation_lowers_the_full_horizon_loss():
+    """The 30-substep inverse problem with the horizon continuation (3 to 30
+    substeps) and the step safeguard: after 40 steps the full-horizon loss is
+    below its starting value, and the control is closer to the hidden grid."""
+    from flowx_gb300.adjoint import InverseProblem
+
+    ip = InverseProblem(scenes.inverse_problem(), substeps=30)
+    losses, control = ip.optimise(steps=40, lr=0.05)
+    assert np.isfinite(losses).all()
+    print(f"continuation, 40 steps: loss {losses[0]:.1f} -> {losses[-1]:.1f} (min {min(losses):.1f})")
+    assert losses[-1] < losses[0]
+    assert float((control - ip.hidden).norm()) < float((ip.initial - ip.hidden).norm())
