@@ -844,6 +844,8 @@ def main():
     ap.add_argument("--case", action="store_true",
                     help="untimed launch-by-launch run of --warmup frames, for profiler captures")
     ap.add_argument("--exact", action="store_true", help="with --case: the reference's float expressions")
+    ap.add_argument("--mesh-collider", action="store_true",
+                    help="with --case: voxelise the large scene's falling sphere from its triangle mesh every frame")
     ap.add_argument("--surface", action="store_true",
                     help="with --case: then the frame's surface twice (splat and marching cubes)")
     args = ap.parse_args()
@@ -865,6 +867,7 @@ def run_case(args):
     separate launch), check the state is finite and exit."""
     import torch
 
+    from flowx_gb300 import scenes
     from flowx_gb300.sph import Solver
 
     torch.cuda.set_device(0)
@@ -873,12 +876,22 @@ def run_case(args):
     sol = Solver(c, scene.positions, scene.velocities, max_cells=c.cell_count,
                  max_collider_voxels=int(np.prod(scene.collider_dims)) if scene.collider_dims else 0,
                  max_surface_samples=scene.surface.sample_count if args.surface else 0, exact=args.exact)
-    if scene.collider_dims is not None:
-        sol.voxelize(scene.primitives_at(0), scene.collider_dims, scene.collider_voxel)
+    def voxelize(frame):
+        if scene.collider_dims is None:
+            return
+        prims = scene.primitives_at(frame)
+        if args.mesh_collider and len(prims) == 1 and prims[0].kind == 0:
+            # the falling sphere from its triangle mesh (flowx_voxelize_meshes)
+            verts, tris = scenes.sphere_mesh(prims[0].r)
+            sol.voxelize_meshes([(verts, tris, scenes.translation(*prims[0].a))], scene.collider_dims,
+                                scene.collider_voxel)
+        else:
+            sol.voxelize(prims, scene.collider_dims, scene.collider_voxel)
+
+    voxelize(0)
     sol._build_grid(0.0)
     for f in range(args.warmup):
-        if scene.collider_dims is not None:
-            sol.voxelize(scene.primitives_at(f), scene.collider_dims, scene.collider_voxel)
+        voxelize(f)
         for _ in range(scene.substeps_per_frame):
             sol._substep(scene.dt)
     if args.surface:

@@ -9,7 +9,14 @@ more: it stays bit-identical to the oracle for the whole run.
 
 Workloads: the 3,200-particle dam break (1 m cube, h 0.1, 48 frames of 4
 substeps, 64^3 splat) and the first 24 of the 307,200-particle pool's 120
-frames (cylinder and wall colliders, 128^3 splat).
+frames (cylinder and wall colliders, 128^3 splat), against the oracle; and
+the stated full lengths - the pool's 120 frames, the 4,000,000-particle large
+scene's 240 frames with the falling sphere re-voxelised on the device every
+frame and the 256^3 splat - against the EXACT path on the GPU. EXACT stands
+in for the oracle there: it equals the oracle bit for bit at these sizes
+(tests/test_gpu_workloads.py, one substep from seeded and mid-run states) and
+over the 48-frame dam break (below), while the oracle would take most of an
+hour for the large run's 960 substeps.
 """
 
 import numpy as np
@@ -72,3 +79,40 @@ def test_fast_full_run_statistics_within_half_percent(name, frames):
     assert np.isfinite(final["positions"]).all()
     err = np.abs(got.mean(0) - want.mean(0)) / np.abs(want.mean(0))
     assert (err <= STAT_TOL).all(), dict(zip(("density", "kinetic_energy", "splat_volume"), err))
+
+
+def _device_run(sc, frames, exact, every):
+    """Per-frame statistics of a run with the collider voxelised on the device
+    every frame (the benchmark's loop), sampled every `every` frames."""
+    from flowx_gb300.sph import Solver
+
+    cfg, dt, surface = sc.config, sc.dt, sc.surface
+    out = []
+    with Solver(cfg, sc.positions, sc.velocities, max_collider_voxels=int(np.prod(sc.collider_dims)),
+                max_surface_samples=surface.sample_count, exact=exact) as s:
+        s._build_grid(0.0)
+        for f in range(frames):
+            s.voxelize(sc.primitives_at(f), sc.collider_dims, sc.collider_voxel)
+            s.step_substeps(dt, sc.substeps_per_frame)
+            if f % every == every - 1:
+                out.append(_stats(s.read("velocities"), s.read("lambda"), s.update_surface(surface, dt), cfg,
+                                  surface))
+        assert np.isfinite(s.read("positions")).all()
+    return np.array(out)
+
+
+@pytest.mark.parametrize("name,frames,every", [("pool", 120, 1), ("large", 240, 2)])
+def test_fast_full_length_run_statistics_against_exact(name, frames, every):
+    sc = getattr(scenes, name)()
+    fast = _device_run(sc, frames, exact=False, every=every)
+    exact = _device_run(sc, frames, exact=True, every=every)
+    err = np.abs(fast.mean(0) - exact.mean(0)) / np.abs(exact.mean(0))
+    print(f"{name} {frames} frames: run-averaged density / kinetic energy / splat volume, FAST vs EXACT: "
+          f"{err[0]:.2e} / {err[1]:.2e} / {err[2]:.2e}")
+    assert (err <= STAT_TOL).all(), dict(zip(("density", "kinetic_energy", "splat_volume"), err))
+    # the reference's own physics check (scripts/smoke_test.py:107-134): mean
+    # density within 15% of rest, here at every sampled frame of the run
+    rest = sc.config.rest_density
+    rel = np.abs(fast[:, 0] - rest) / rest
+    print(f"{name}: mean density off rest by at most {rel.max():.3f}")
+    assert (rel < 0.15).all()
