@@ -10,6 +10,7 @@ import bench
 
 
 def _tree(tmp_path, digest):
+    os.symlink(os.path.join(os.path.dirname(bench.__file__), "flowx_gb300"), tmp_path / "flowx_gb300")
     prof = tmp_path / "profiles"
     prof.mkdir()
     (prof / "traffic.json").write_text(json.dumps({
@@ -26,9 +27,7 @@ def test_capture_used_only_for_the_sources_it_was_taken_of(tmp_path, monkeypatch
 
 def test_capture_of_the_current_sources_is_used(tmp_path, monkeypatch):
     digest = bench.kernel_source_digest()  # of the repository's flowx_gb300/csrc
-    root = _tree(tmp_path, digest)
-    os.symlink(os.path.join(os.path.dirname(bench.__file__), "flowx_gb300"), root / "flowx_gb300")
-    monkeypatch.setattr(bench, "ROOT", str(root))
+    monkeypatch.setattr(bench, "ROOT", str(_tree(tmp_path, digest)))
     rec = bench._capture_of_this_build()
     assert rec["bytes_per_launch"]["lambda"] == 123
     assert rec["warp_instructions_per_launch"]["lambda"] == 456
