@@ -49,3 +49,16 @@ def test_python_binding_signatures(lib):
     assert loaded.flowx_substep.argtypes is not None
     assert ctypes.sizeof(_lib.Push) == 128
     assert ctypes.sizeof(_lib.Primitive) == 64
+
+
+def test_python_flag_values_match_the_header():
+    """The flag bits and the warp-pass threshold the Python binding passes are
+    the ones include/flowx.h defines."""
+    from flowx_gb300 import _lib
+
+    text = open(os.path.join(ROOT, "include", "flowx.h")).read()
+    for name in ("KEEP_DELTA", "EXACT", "REFERENCE_ORDER", "WARP_PASSES", "THREAD_PASSES"):
+        m = re.search(rf"FLOWX_FLAG_{name}\s*=\s*(\d+)", text)
+        assert m and int(m.group(1)) == getattr(_lib, f"FLAG_{name}"), name
+    m = re.search(r"#define FLOWX_WARP_PASSES_MAX_PARTICLES\s+(\d+)", text)
+    assert m and int(m.group(1)) == _lib.WARP_PASSES_MAX_PARTICLES
