@@ -51,16 +51,20 @@ ADJOINT_SUBSTEPS = 30  # the inverse problem's rollout
 
 # Algorithmic bytes per particle and launch of each kernel (compulsory HBM
 # traffic: every array touched once per launch, neighbour reuse served on chip;
-# float4 pos/vel/pred/normal, float2 (density, lambda) of which the kernel
-# needs the lanes it reads, u32 keys/ids/ranks, u64 sort pairs).
+# float4 pos/vel/pred/normal, float2 (density, lambda), u32 keys/ids/ranks, u64
+# sort pairs). The neighbour passes take the per-pass figures of the
+# reference's path (one row per pass: normal 44, lambda 28, delta with its
+# ping-pong apply 44, velocity + XSPH + finalize 77), which also count the u32
+# key each particle's slot carries; the grid-build kernels, which split that
+# path's predict/sort rows differently, count their own arrays.
 BYTES_PER_PARTICLE = {
-    "normal": 16 + 4 + 16,            # pred, density_j, normal out
+    "normal": 44,
     "predict_key": 16 + 16 + 16 + 4 + 4,  # pos, vel, normal; key, rank out
     "scatter": 4 + 4 + 4 + 8,         # key, rank, id; pair out
     "permute_step": 8 + 16 + 16 + 16 + 4 + 16 + 16 + 4 + 4,  # pair, pos, vel, normal, key; pos, pred, id, key out
-    "lambda": 16 + 8,                 # pred; (density, lambda) out
-    "delta_apply": 16 + 4 + 16,       # pred, lambda_j; pred out
-    "xsph_finalize": 16 + 16 + 4 + 16 + 16,  # pred, pos, density_j; pos, vel out
+    "lambda": 28,
+    "delta_apply": 44,
+    "xsph_finalize": 77,
     "cell_sort_small": 16,            # pairs in + out
 }
 
