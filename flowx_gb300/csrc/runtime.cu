@@ -277,6 +277,8 @@ int Ctx::upload_segs(const std::vector<SegParams> &s, int cells)
     segs_uploaded = true;
     d.segs = d_segs;
     d.nseg = (int)segs.size();
+    d.seg0 = segs.empty() ? SegParams{} : segs[0];
+    drop_graphs();  // their launches carry seg0
   }
   if (cells != d.cells) {
     if (have_grid && cells != d.cells) have_grid = false;

@@ -236,7 +236,10 @@ int flowx_build_grid(flowx_ctx *ctx, const flowx_push *push);
 int flowx_substep(flowx_ctx *ctx, const flowx_push *push, int iterations);
 
 /* `substeps` substeps as one CUDA-graph launch (captured on first use for a
- * given shape). Replaces the substep loop of solver/sph.py:517-530 (_step). */
+ * given shape). Replaces the substep loop of solver/sph.py:517-530 (_step).
+ * A single-scene context's graphs carry the scene's parameters, so a push
+ * block whose values differ from the previous call's (dt, h, ...) re-captures
+ * them; an unchanged push block reuses them. */
 int flowx_step(flowx_ctx *ctx, const flowx_push *push, int iterations, int substeps);
 
 /* One reference pass on the current buffers, as one gpu.compute.dispatch of
