@@ -23,11 +23,15 @@
 // substep's kernels take from their by-value DeviceState argument instead
 // (DeviceState::seg0): the arithmetic then reads them as constant operands,
 // with no load and no register (6-11% per neighbour pass on the 4M-particle
-// workload).
+// workload). A batch reads them from its slice of a constant-memory copy of
+// the table (c_segs) when one is free, through the constant cache instead of
+// L1 (3.8% on the 64-scene batched workload); otherwise from the device table.
 #pragma once
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include <type_traits>
 
 namespace flowx {
 
@@ -163,6 +167,7 @@ struct DeviceState {
   int bitonic_n;            // next power of two >= n (the reference's sorted_count)
   const SegParams *segs;
   SegParams seg0;           // segs[0], read from the kernel argument by single-scene launches
+  int cseg_base;            // this context's first entry of c_segs, or -1 (not there)
   int32_t *slot_seg;        // per slot: its segment (read only when nseg > 1)
   int nseg;
   int warp_passes;          // neighbour passes one warp per particle (pbf_warp.cu), else one thread
@@ -180,16 +185,46 @@ __device__ __forceinline__ int slot_segment(const DeviceState &d, int k)
   return d.nseg == 1 ? 0 : __ldg(&d.slot_seg[k]);
 }
 
-// Parameters of slot k's segment; ONE_SEG (a single-scene context) takes them
-// from the kernel argument, whose fields the arithmetic reads as constants.
-template <bool ONE_SEG>
+// Where a kernel reads its slot's segment parameters: the device table, the
+// kernel argument (a single-scene context: seg0), or the context's slice of
+// a constant-memory copy of the table (a batch whose table fits it).
+enum SegSource { kSegTable = 0, kSegArg = 1, kSegConst = 2 };
+constexpr int kConstSegs = 128;
+// One copy per translation unit (no relocatable device code); the units that
+// launch substep kernels each export an upload (const_segs_upload_*).
+static __constant__ SegParams c_segs[kConstSegs];
+
+template <int SEG>
 __device__ __forceinline__ const SegParams &slot_params(const DeviceState &d, int k)
 {
-  if constexpr (ONE_SEG)
+  if constexpr (SEG == kSegArg)
     return d.seg0;
+  else if constexpr (SEG == kSegConst)
+    return c_segs[d.cseg_base + slot_segment(d, k)];
   else
     return d.segs[slot_segment(d, k)];
 }
+
+inline int seg_source(const DeviceState &d)
+{
+  return d.nseg == 1 ? kSegArg : (d.cseg_base >= 0 ? kSegConst : kSegTable);
+}
+
+// f(std::integral_constant<int, SEG>) for the context's source.
+template <class F>
+inline void with_seg_source(const DeviceState &d, F &&f)
+{
+  switch (seg_source(d)) {
+    case kSegArg: f(std::integral_constant<int, kSegArg>{}); break;
+    case kSegConst: f(std::integral_constant<int, kSegConst>{}); break;
+    default: f(std::integral_constant<int, kSegTable>{}); break;
+  }
+}
+
+// The constant copies of the segment table (entries [base, base + n)).
+cudaError_t const_segs_upload_pbf(int base, const SegParams *s, int n, cudaStream_t st);
+cudaError_t const_segs_upload_warp(int base, const SegParams *s, int n, cudaStream_t st);
+cudaError_t const_segs_upload_grid(int base, const SegParams *s, int n, cudaStream_t st);
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 

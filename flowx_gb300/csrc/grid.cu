@@ -44,14 +44,14 @@ __device__ __forceinline__ void count_key(uint32_t *counts, uint32_t key, bool a
 
 // Fused substep: pos/vel/normal -> key, rank (the predicted position itself is
 // recomputed by the permute, which is cheaper than storing and re-reading it).
-template <bool ONE_SEG>
+template <int SEG>
 __global__ void k_predict_key(DeviceState d, const float4 *__restrict__ normal_in)
 {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = k < d.n;
   uint32_t key = 0;
   if (active) {
-    const SegParams &s = slot_params<ONE_SEG>(d, k);
+    const SegParams &s = slot_params<SEG>(d, k);
     const float4 p = d.pos[k];
     const float4 v = d.vel[k];
     const float4 n = s.sigma > 0.0f ? normal_in[k] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -85,11 +85,18 @@ __global__ void k_key_only(DeviceState d, const float4 *__restrict__ pred)
 
 void launch_predict_key(const DeviceState &d, const float4 *normal_in, cudaStream_t st)
 {
-  const bool one = d.nseg == 1;
-  const int b = FLOWX_BLOCK(d, K_PREDICT_KEY, 256, one ? (const void *)k_predict_key<true> : (const void *)k_predict_key<false>);
   if (d.n <= 0) return;
-  if (one) k_predict_key<true><<<grid_for(d.n, b), b, 0, st>>>(d, normal_in);
-  else k_predict_key<false><<<grid_for(d.n, b), b, 0, st>>>(d, normal_in);
+  with_seg_source(d, [&](auto tag) {
+    constexpr int SEG = decltype(tag)::value;
+    const int b = FLOWX_BLOCK(d, K_PREDICT_KEY, 256, (const void *)k_predict_key<SEG>);
+    k_predict_key<SEG><<<grid_for(d.n, b), b, 0, st>>>(d, normal_in);
+  });
+}
+
+cudaError_t const_segs_upload_grid(int base, const SegParams *s, int n, cudaStream_t st)
+{
+  return cudaMemcpyToSymbolAsync(c_segs, s, sizeof(SegParams) * n, sizeof(SegParams) * base, cudaMemcpyHostToDevice,
+                                 st);
 }
 
 void launch_key_only(const DeviceState &d, const float4 *pred, cudaStream_t st)
@@ -391,14 +398,14 @@ int launch_reference_order(const DeviceState &d, cudaStream_t st)
 // the substep's normal (computed into scratch in the old order) moved to the
 // new slot, and the slot's key and id recorded. Velocity and lambda need no
 // copy: the rest of the substep rewrites them before reading.
-template <bool ONE_SEG>
+template <int SEG>
 __global__ void k_permute_step(DeviceState d, float4 *__restrict__ pred_out, const float4 *__restrict__ normal_in)
 {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= d.n) return;
   const unsigned long long pr = d.pairs[k];
   const int s = (int)(uint32_t)pr;
-  const SegParams &sp = slot_params<ONE_SEG>(d, k);
+  const SegParams &sp = slot_params<SEG>(d, k);
   const float4 p = d.pos[s];
   const float4 v = d.vel[s];
   const float4 n = sp.sigma > 0.0f ? normal_in[s] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -414,12 +421,12 @@ __global__ void k_permute_step(DeviceState d, float4 *__restrict__ pred_out, con
 
 void launch_permute_step(const DeviceState &d, float4 *pred_out, const float4 *normal_in, cudaStream_t st)
 {
-  const bool one = d.nseg == 1;
-  const int b =
-      FLOWX_BLOCK(d, K_PERMUTE_STEP, 256, one ? (const void *)k_permute_step<true> : (const void *)k_permute_step<false>);
   if (d.n <= 0) return;
-  if (one) k_permute_step<true><<<grid_for(d.n, b), b, 0, st>>>(d, pred_out, normal_in);
-  else k_permute_step<false><<<grid_for(d.n, b), b, 0, st>>>(d, pred_out, normal_in);
+  with_seg_source(d, [&](auto tag) {
+    constexpr int SEG = decltype(tag)::value;
+    const int b = FLOWX_BLOCK(d, K_PERMUTE_STEP, 256, (const void *)k_permute_step<SEG>);
+    k_permute_step<SEG><<<grid_for(d.n, b), b, 0, st>>>(d, pred_out, normal_in);
+  });
 }
 
 // Standalone grid build: every per-particle array moves to its new slot

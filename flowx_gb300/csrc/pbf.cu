@@ -30,7 +30,7 @@ static inline unsigned grid_for(long long n, int b) { return (unsigned)((n + b -
 #define FLOWX_SLOT_PROLOGUE_SEG                        \
   const int i = blockIdx.x * blockDim.x + threadIdx.x; \
   if (i >= d.n) return;                                \
-  const SegParams &s = slot_params<ONE_SEG>(d, i);
+  const SegParams &s = slot_params<SEG>(d, i);
 
 // ---- neighbour passes -------------------------------------------------------
 
@@ -40,7 +40,7 @@ static inline unsigned grid_for(long long n, int b) { return (unsigned)((n + b -
 // latency than the few registers cost, 1.6% per frame), delta_apply four
 // (32), XSPH five 256-thread blocks (48).
 // sph_lambda.glsl:17-77
-template <bool EXACT, bool ONE_SEG>
+template <bool EXACT, int SEG>
 __global__ void __launch_bounds__(512, 3) k_lambda_f(DeviceState d, const float4 *__restrict__ pred)
 {
   FLOWX_SLOT_PROLOGUE_SEG
@@ -123,7 +123,7 @@ __device__ __forceinline__ void normal_terms(const SegParams &s, float rho_j, fl
 // gathers are latency-bound, and the full 64 resident warps hide more of them
 // (0.726 -> 0.688 ms per launch on the 4M-particle workload); the reference
 // form would spill at 32 and keeps three.
-template <bool EXACT, bool ONE_SEG>
+template <bool EXACT, int SEG>
 __global__ void __launch_bounds__(512, EXACT ? 3 : 4) k_delta_apply_f(DeviceState d, const float4 *__restrict__ pred_in,
                                                        float4 *__restrict__ pred_out, int last)
 {
@@ -219,7 +219,7 @@ __device__ __forceinline__ float3 xsph_sum_f(const SegParams &s, const DeviceSta
 // of this grid, which the next substep's permute maps to its own). Bounded to
 // five 256-thread blocks per SM (48 registers): with both bodies it spills at
 // 40 (1.68 -> 1.63 ms per launch on the 4M-particle workload).
-template <bool EXACT, bool NORMALS, bool ONE_SEG>
+template <bool EXACT, bool NORMALS, int SEG>
 __global__ void __launch_bounds__(256, 5) k_xsph_finalize_f(DeviceState d, const float4 *__restrict__ pred,
                                                          float4 *__restrict__ pos_out, int keep_delta)
 {
@@ -240,7 +240,7 @@ __global__ void __launch_bounds__(256, 5) k_xsph_finalize_f(DeviceState d, const
 // sph_normal.glsl:24-81 (over the previous substep's grid, as the reference);
 // the fused substep runs it only when the previous substep's XSPH pass did
 // not already evaluate it (the first substep, or state changed in between).
-template <bool EXACT, bool ONE_SEG>
+template <bool EXACT, int SEG>
 __global__ void __launch_bounds__(512, 3) k_normal_f(DeviceState d, const float4 *__restrict__ pred,
                                                   float4 *__restrict__ out)
 {
@@ -266,34 +266,30 @@ __global__ void __launch_bounds__(512, 3) k_normal_f(DeviceState d, const float4
 void launch_lambda_f(const DeviceState &d, const float4 *pred, bool exact, cudaStream_t st)
 {
   if (d.warp_passes) return launch_lambda_w(d, pred, exact, st);
-  const bool one = d.nseg == 1;
-  const void *fn = exact ? (one ? (const void *)k_lambda_f<true, true> : (const void *)k_lambda_f<true, false>)
-                         : (one ? (const void *)k_lambda_f<false, true> : (const void *)k_lambda_f<false, false>);
-  const int b = FLOWX_BLOCK(d, K_LAMBDA, 128, fn);
   if (d.n <= 0) return;
-  const unsigned g = grid_for(d.n, b);
-  const size_t sm = row_mask_bytes(b);
-  if (exact && one) k_lambda_f<true, true><<<g, b, sm, st>>>(d, pred);
-  else if (exact) k_lambda_f<true, false><<<g, b, sm, st>>>(d, pred);
-  else if (one) k_lambda_f<false, true><<<g, b, sm, st>>>(d, pred);
-  else k_lambda_f<false, false><<<g, b, sm, st>>>(d, pred);
+  with_seg_source(d, [&](auto tag) {
+    constexpr int SEG = decltype(tag)::value;
+    const void *fn = exact ? (const void *)k_lambda_f<true, SEG> : (const void *)k_lambda_f<false, SEG>;
+    const int b = FLOWX_BLOCK(d, K_LAMBDA, 128, fn);
+    const unsigned g = grid_for(d.n, b);
+    if (exact) k_lambda_f<true, SEG><<<g, b, row_mask_bytes(b), st>>>(d, pred);
+    else k_lambda_f<false, SEG><<<g, b, row_mask_bytes(b), st>>>(d, pred);
+  });
 }
 void launch_delta_apply_f(const DeviceState &d, const float4 *pred_in, float4 *pred_out, bool exact, bool last,
                           cudaStream_t st)
 {
   if (d.warp_passes) return launch_delta_apply_w(d, pred_in, pred_out, exact, last, st);
-  const bool one = d.nseg == 1;
-  const void *fn = exact ? (one ? (const void *)k_delta_apply_f<true, true> : (const void *)k_delta_apply_f<true, false>)
-                         : (one ? (const void *)k_delta_apply_f<false, true> : (const void *)k_delta_apply_f<false, false>);
-  const int b = FLOWX_BLOCK(d, K_DELTA_APPLY, 128, fn);
   if (d.n <= 0) return;
   const int l = last ? 1 : 0;
-  const unsigned g = grid_for(d.n, b);
-  const size_t sm = row_mask_bytes(b);
-  if (exact && one) k_delta_apply_f<true, true><<<g, b, sm, st>>>(d, pred_in, pred_out, l);
-  else if (exact) k_delta_apply_f<true, false><<<g, b, sm, st>>>(d, pred_in, pred_out, l);
-  else if (one) k_delta_apply_f<false, true><<<g, b, sm, st>>>(d, pred_in, pred_out, l);
-  else k_delta_apply_f<false, false><<<g, b, sm, st>>>(d, pred_in, pred_out, l);
+  with_seg_source(d, [&](auto tag) {
+    constexpr int SEG = decltype(tag)::value;
+    const void *fn = exact ? (const void *)k_delta_apply_f<true, SEG> : (const void *)k_delta_apply_f<false, SEG>;
+    const int b = FLOWX_BLOCK(d, K_DELTA_APPLY, 128, fn);
+    const unsigned g = grid_for(d.n, b);
+    if (exact) k_delta_apply_f<true, SEG><<<g, b, row_mask_bytes(b), st>>>(d, pred_in, pred_out, l);
+    else k_delta_apply_f<false, SEG><<<g, b, row_mask_bytes(b), st>>>(d, pred_in, pred_out, l);
+  });
 }
 void launch_xsph_inputs(const DeviceState &d, const float4 *pred, bool exact, cudaStream_t st)
 {
@@ -305,14 +301,13 @@ template <bool EXACT, bool NORMALS>
 static void xsph_finalize_launch(const DeviceState &d, const float4 *pred, float4 *pos_out, int keep_delta,
                                  cudaStream_t st)
 {
-  const bool one = d.nseg == 1;
-  const void *fn = one ? (const void *)k_xsph_finalize_f<EXACT, NORMALS, true>
-                       : (const void *)k_xsph_finalize_f<EXACT, NORMALS, false>;
-  const int b = FLOWX_BLOCK(d, K_XSPH_FINALIZE, 128, fn);
-  const unsigned g = grid_for(d.n, b);
-  const size_t sm = row_mask_bytes(b);
-  if (one) k_xsph_finalize_f<EXACT, NORMALS, true><<<g, b, sm, st>>>(d, pred, pos_out, keep_delta);
-  else k_xsph_finalize_f<EXACT, NORMALS, false><<<g, b, sm, st>>>(d, pred, pos_out, keep_delta);
+  with_seg_source(d, [&](auto tag) {
+    constexpr int SEG = decltype(tag)::value;
+    const void *fn = (const void *)k_xsph_finalize_f<EXACT, NORMALS, SEG>;
+    const int b = FLOWX_BLOCK(d, K_XSPH_FINALIZE, 128, fn);
+    k_xsph_finalize_f<EXACT, NORMALS, SEG><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred, pos_out,
+                                                                                           keep_delta);
+  });
 }
 void launch_xsph_finalize_f(const DeviceState &d, const float4 *pred, float4 *pos_out, bool keep_delta, bool exact,
                             bool normals, cudaStream_t st)
@@ -328,17 +323,21 @@ void launch_xsph_finalize_f(const DeviceState &d, const float4 *pred, float4 *po
 void launch_normal_f(const DeviceState &d, const float4 *pred, float4 *out, bool exact, cudaStream_t st)
 {
   if (d.warp_passes) return launch_normal_w(d, pred, out, exact, st);
-  const bool one = d.nseg == 1;
-  const void *fn = exact ? (one ? (const void *)k_normal_f<true, true> : (const void *)k_normal_f<true, false>)
-                         : (one ? (const void *)k_normal_f<false, true> : (const void *)k_normal_f<false, false>);
-  const int b = FLOWX_BLOCK(d, K_NORMAL, 128, fn);
   if (d.n <= 0) return;
-  const unsigned g = grid_for(d.n, b);
-  const size_t sm = row_mask_bytes(b);
-  if (exact && one) k_normal_f<true, true><<<g, b, sm, st>>>(d, pred, out);
-  else if (exact) k_normal_f<true, false><<<g, b, sm, st>>>(d, pred, out);
-  else if (one) k_normal_f<false, true><<<g, b, sm, st>>>(d, pred, out);
-  else k_normal_f<false, false><<<g, b, sm, st>>>(d, pred, out);
+  with_seg_source(d, [&](auto tag) {
+    constexpr int SEG = decltype(tag)::value;
+    const void *fn = exact ? (const void *)k_normal_f<true, SEG> : (const void *)k_normal_f<false, SEG>;
+    const int b = FLOWX_BLOCK(d, K_NORMAL, 128, fn);
+    const unsigned g = grid_for(d.n, b);
+    if (exact) k_normal_f<true, SEG><<<g, b, row_mask_bytes(b), st>>>(d, pred, out);
+    else k_normal_f<false, SEG><<<g, b, row_mask_bytes(b), st>>>(d, pred, out);
+  });
+}
+
+cudaError_t const_segs_upload_pbf(int base, const SegParams *s, int n, cudaStream_t st)
+{
+  return cudaMemcpyToSymbolAsync(c_segs, s, sizeof(SegParams) * n, sizeof(SegParams) * base, cudaMemcpyHostToDevice,
+                                 st);
 }
 
 // ---- single reference passes (per-pass API; always exact) ------------------

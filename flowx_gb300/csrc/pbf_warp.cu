@@ -91,12 +91,12 @@ __device__ __forceinline__ float shfl(float v, int l) { return __shfl_sync(kFull
   const int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); \
   if (i >= d.n) return;                                              \
   const int lane = threadIdx.x & 31;                                 \
-  const SegParams &s = slot_params<ONE_SEG>(d, i);
+  const SegParams &s = slot_params<SEG>(d, i);
 
 // sph_lambda.glsl:17-77; LambdaAcc's operations (neighbour.cuh), folded per
 // candidate: the density term for every candidate within h, the gradient
 // terms for those with r^2 > 1e-12.
-template <bool EXACT, bool ONE_SEG>
+template <bool EXACT, int SEG>
 __global__ void __launch_bounds__(kWarpBlock) k_lambda_w(DeviceState d, const float4 *__restrict__ pred)
 {
   FLOWX_WARP_PROLOGUE
@@ -170,7 +170,7 @@ __global__ void __launch_bounds__(kWarpBlock) k_lambda_w(DeviceState d, const fl
 
 // sph_delta.glsl:19-85 + sph_apply_delta.glsl; delta_pair's operations
 // (neighbour.cuh), folded per candidate with 1e-12 < r^2 < h^2.
-template <bool EXACT, bool ONE_SEG>
+template <bool EXACT, int SEG>
 __global__ void __launch_bounds__(kWarpBlock) k_delta_apply_w(DeviceState d, const float4 *__restrict__ pred_in,
                                                               float4 *__restrict__ pred_out, int last)
 {
@@ -290,7 +290,7 @@ struct NormalTerm {
 // sph_velocity.glsl + sph_xsph.glsl + sph_finalize.glsl as k_xsph_finalize_f
 // (pbf.cu), neighbour velocities and densities from d.xv; NORMALS: also the
 // next substep's normal pass into d.normal_alt.
-template <bool EXACT, bool NORMALS, bool ONE_SEG>
+template <bool EXACT, bool NORMALS, int SEG>
 __global__ void __launch_bounds__(kWarpBlock) k_xsph_finalize_w(DeviceState d, const float4 *__restrict__ pred,
                                                                 float4 *__restrict__ pos_out, int keep_delta)
 {
@@ -358,7 +358,7 @@ __global__ void __launch_bounds__(kWarpBlock) k_xsph_finalize_w(DeviceState d, c
 }
 
 // sph_normal.glsl:24-81 as k_normal_f (pbf.cu).
-template <bool EXACT, bool ONE_SEG>
+template <bool EXACT, int SEG>
 __global__ void __launch_bounds__(kWarpBlock) k_normal_w(DeviceState d, const float4 *__restrict__ pred,
                                                          float4 *__restrict__ out)
 {
@@ -387,36 +387,33 @@ __global__ void __launch_bounds__(kWarpBlock) k_normal_w(DeviceState d, const fl
 
 }  // namespace
 
-// Single-scene contexts (nseg == 1) take the scene's parameters from the
-// kernel argument (slot_params).
 void launch_lambda_w(const DeviceState &d, const float4 *pred, bool exact, cudaStream_t st)
 {
   if (d.n <= 0) return;
-  const unsigned g = warp_grid(d.n);
-  const bool one = d.nseg == 1;
-  if (exact && one) k_lambda_w<true, true><<<g, kWarpBlock, 0, st>>>(d, pred);
-  else if (exact) k_lambda_w<true, false><<<g, kWarpBlock, 0, st>>>(d, pred);
-  else if (one) k_lambda_w<false, true><<<g, kWarpBlock, 0, st>>>(d, pred);
-  else k_lambda_w<false, false><<<g, kWarpBlock, 0, st>>>(d, pred);
+  with_seg_source(d, [&](auto tag) {
+    constexpr int SEG = decltype(tag)::value;
+    if (exact) k_lambda_w<true, SEG><<<warp_grid(d.n), kWarpBlock, 0, st>>>(d, pred);
+    else k_lambda_w<false, SEG><<<warp_grid(d.n), kWarpBlock, 0, st>>>(d, pred);
+  });
 }
 void launch_delta_apply_w(const DeviceState &d, const float4 *pred_in, float4 *pred_out, bool exact, bool last,
                           cudaStream_t st)
 {
   if (d.n <= 0) return;
-  const unsigned g = warp_grid(d.n);
-  const bool one = d.nseg == 1;
   const int l = last ? 1 : 0;
-  if (exact && one) k_delta_apply_w<true, true><<<g, kWarpBlock, 0, st>>>(d, pred_in, pred_out, l);
-  else if (exact) k_delta_apply_w<true, false><<<g, kWarpBlock, 0, st>>>(d, pred_in, pred_out, l);
-  else if (one) k_delta_apply_w<false, true><<<g, kWarpBlock, 0, st>>>(d, pred_in, pred_out, l);
-  else k_delta_apply_w<false, false><<<g, kWarpBlock, 0, st>>>(d, pred_in, pred_out, l);
+  with_seg_source(d, [&](auto tag) {
+    constexpr int SEG = decltype(tag)::value;
+    if (exact) k_delta_apply_w<true, SEG><<<warp_grid(d.n), kWarpBlock, 0, st>>>(d, pred_in, pred_out, l);
+    else k_delta_apply_w<false, SEG><<<warp_grid(d.n), kWarpBlock, 0, st>>>(d, pred_in, pred_out, l);
+  });
 }
 template <bool EXACT, bool NORMALS>
 static void xsph_finalize_w_launch(const DeviceState &d, const float4 *pred, float4 *pos_out, int kd, cudaStream_t st)
 {
-  const unsigned g = warp_grid(d.n);
-  if (d.nseg == 1) k_xsph_finalize_w<EXACT, NORMALS, true><<<g, kWarpBlock, 0, st>>>(d, pred, pos_out, kd);
-  else k_xsph_finalize_w<EXACT, NORMALS, false><<<g, kWarpBlock, 0, st>>>(d, pred, pos_out, kd);
+  with_seg_source(d, [&](auto tag) {
+    constexpr int SEG = decltype(tag)::value;
+    k_xsph_finalize_w<EXACT, NORMALS, SEG><<<warp_grid(d.n), kWarpBlock, 0, st>>>(d, pred, pos_out, kd);
+  });
 }
 void launch_xsph_finalize_w(const DeviceState &d, const float4 *pred, float4 *pos_out, bool keep_delta, bool exact,
                             bool normals, cudaStream_t st)
@@ -431,12 +428,17 @@ void launch_xsph_finalize_w(const DeviceState &d, const float4 *pred, float4 *po
 void launch_normal_w(const DeviceState &d, const float4 *pred, float4 *out, bool exact, cudaStream_t st)
 {
   if (d.n <= 0) return;
-  const unsigned g = warp_grid(d.n);
-  const bool one = d.nseg == 1;
-  if (exact && one) k_normal_w<true, true><<<g, kWarpBlock, 0, st>>>(d, pred, out);
-  else if (exact) k_normal_w<true, false><<<g, kWarpBlock, 0, st>>>(d, pred, out);
-  else if (one) k_normal_w<false, true><<<g, kWarpBlock, 0, st>>>(d, pred, out);
-  else k_normal_w<false, false><<<g, kWarpBlock, 0, st>>>(d, pred, out);
+  with_seg_source(d, [&](auto tag) {
+    constexpr int SEG = decltype(tag)::value;
+    if (exact) k_normal_w<true, SEG><<<warp_grid(d.n), kWarpBlock, 0, st>>>(d, pred, out);
+    else k_normal_w<false, SEG><<<warp_grid(d.n), kWarpBlock, 0, st>>>(d, pred, out);
+  });
+}
+
+cudaError_t const_segs_upload_warp(int base, const SegParams *s, int n, cudaStream_t st)
+{
+  return cudaMemcpyToSymbolAsync(c_segs, s, sizeof(SegParams) * n, sizeof(SegParams) * base, cudaMemcpyHostToDevice,
+                                 st);
 }
 
 }  // namespace flowx

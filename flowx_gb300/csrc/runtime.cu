@@ -33,6 +33,36 @@ static const char *kKernelNames[K_COUNT] = {
     "finalize",      "permute_all",  "gather",      "scatter_ids",  "voxelize",     "bitonic_sort",
 };
 
+// Slices of the constant copy of the segment table, per device: a batch
+// context reserves one entry per scene; none left, it reads the device table.
+static std::mutex g_cseg_mu;
+static std::map<int, std::vector<char>> g_cseg_used;
+
+static int cseg_reserve(int dev, int n)
+{
+  std::lock_guard<std::mutex> lk(g_cseg_mu);
+  auto &used = g_cseg_used[dev];
+  if (used.empty()) used.assign(kConstSegs, 0);
+  for (int b = 0; b + n <= kConstSegs; ++b) {
+    int k = 0;
+    while (k < n && !used[b + k]) ++k;
+    if (k == n) {
+      for (int j = 0; j < n; ++j) used[b + j] = 1;
+      return b;
+    }
+    b += k;
+  }
+  return -1;
+}
+
+static void cseg_release(int dev, int base, int n)
+{
+  if (base < 0 || n <= 0) return;
+  std::lock_guard<std::mutex> lk(g_cseg_mu);
+  auto &used = g_cseg_used[dev];
+  for (int j = 0; j < n && base + j < (int)used.size(); ++j) used[base + j] = 0;
+}
+
 int kernel_max_threads(const void *kernel)
 {
   static std::mutex mu;
@@ -170,6 +200,7 @@ int Ctx::allocate()
   if (e != cudaSuccess) return cuda(e, "device allocation");
   d.segs = d_segs;
   d.nseg = (int)segs.size();
+  d.cseg_base = -1;
   d.n = total_particles;
   d.cells = 0;
   d.warp_passes = (flags & FLOWX_FLAG_WARP_PASSES) ? 1
@@ -184,6 +215,9 @@ int Ctx::allocate()
 
 void Ctx::release()
 {
+  cseg_release(device, d.cseg_base, cseg_count);
+  d.cseg_base = -1;
+  cseg_count = 0;
   for (auto &kv : graphs) {
     cudaGraphExecDestroy(kv.second.exec);
   }
@@ -278,6 +312,20 @@ int Ctx::upload_segs(const std::vector<SegParams> &s, int cells)
     d.segs = d_segs;
     d.nseg = (int)segs.size();
     d.seg0 = segs.empty() ? SegParams{} : segs[0];
+    if (segs.size() > 1) {
+      const int need = (int)segs.size();
+      if (need > cseg_count) {
+        cseg_release(device, d.cseg_base, cseg_count);
+        d.cseg_base = cseg_reserve(device, need);
+        cseg_count = d.cseg_base >= 0 ? need : 0;
+      }
+      if (d.cseg_base >= 0) {
+        cudaError_t e = const_segs_upload_pbf(d.cseg_base, segs.data(), need, stream);
+        if (e == cudaSuccess) e = const_segs_upload_warp(d.cseg_base, segs.data(), need, stream);
+        if (e == cudaSuccess) e = const_segs_upload_grid(d.cseg_base, segs.data(), need, stream);
+        if (e != cudaSuccess) return cuda(e, "constant segment table upload");
+      }
+    }
     drop_graphs();  // their launches carry seg0
   }
   if (cells != d.cells) {

@@ -44,6 +44,7 @@ struct Ctx {
   std::vector<SegParams> segs;
   bool segs_uploaded = false;
   size_t seg_capacity = 1;         // entries the device segment table holds
+  int cseg_count = 0;              // entries of the constant table reserved (base in d.cseg_base)
   int pred_idx = 0;                // predicted positions live in pred_a (0) or pred_b (1)
   bool have_grid = false;          // keys / ids / offsets describe a built grid
   bool offsets_dirty = false;      // keys were uploaded; offsets follow on the next push

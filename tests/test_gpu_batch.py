@@ -45,6 +45,31 @@ def test_batch_equals_scenes_stepped_alone(graph):
                 np.testing.assert_array_equal(arr[lo:hi], one.read(name), err_msg=f"scene {k} {name}")
 
 
+def test_batch_beyond_the_constant_segment_table():
+    """A batch reads its scenes' parameters from its slice of a constant-memory
+    copy of the segment table (128 entries per device), or from the device
+    table when the slice does not fit. 130 scenes take the device table; the
+    same scenes as two batches of 65, one after the other, each take a slice.
+    The substeps are the same bit for bit (the re-associated arithmetic)."""
+    from flowx_gb300.batch import Batch
+
+    sc = scenes.batched_scenes(count=130, seed=7, n_range=(200, 600))
+    nsub = 2
+    with Batch(sc) as b:
+        b.build_grid()
+        b.step(4, nsub)
+        want = {name: b.read(name) for name in ("positions", "velocities", "lambda")}
+    lo = 0
+    for part in (sc[:65], sc[65:]):
+        n = sum(x.n for x in part)
+        with Batch(part) as b:
+            b.build_grid()
+            b.step(4, nsub)
+            for name, arr in want.items():
+                np.testing.assert_array_equal(b.read(name), arr[lo:lo + n], err_msg=name)
+        lo += n
+
+
 def test_batch_scene_matches_oracle():
     from flowx_gb300.batch import Batch
 
