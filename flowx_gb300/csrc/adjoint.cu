@@ -1051,6 +1051,8 @@ struct Adjoint {
   {
     d.segs = d_seg;
     d.nseg = 1;
+    d.seg0 = seg;
+    d.cseg_base = -1;
     d.n = n;
     d.cells = cells;
     d.sm_count = sm_count;

@@ -188,6 +188,8 @@ int flowx_build_grid_static(const float *predicted, int32_t particle_count, cons
   s.p_begin = 0;
   s.c_begin = 0;
   s.col_begin = 0;
+  d.seg0 = s;
+  d.cseg_base = -1;
   cudaError_t e = cudaMemsetAsync(d.counts, 0, sizeof(uint32_t) * (size_t)cells, st);
   if (e != cudaSuccess) return fail(FLOWX_ERR_CUDA, std::string("flowx_build_grid_static: ") + cudaGetErrorString(e));
   k_store_seg<<<1, 1, 0, st>>>(segs, s);
