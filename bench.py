@@ -320,7 +320,7 @@ def kernel_source_digest() -> str:
     return h.hexdigest()
 
 
-def _capture_of_this_build():
+def _capture_of_current_sources():
     """Per-launch DRAM bytes and warp instructions of the dominant kernels
     from the committed summary of an ncu capture (profiles/traffic.json),
     used only when that capture was taken of exactly these kernel sources;
@@ -678,7 +678,7 @@ def run_flowx(args):
     dom_bytes = BYTES_PER_PARTICLE.get(dominant, 0) * scene.n
     dom_ms = prof[dominant][0] / prof[dominant][1]
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
-    capture = _capture_of_this_build()
+    capture = _capture_of_current_sources()
     traffic = capture.get("bytes_per_launch", {}).get(dominant) if capture else None
     warp_inst = capture.get("warp_instructions_per_launch", {}).get(dominant) if capture else None
     roofline = {
@@ -690,7 +690,7 @@ def run_flowx(args):
         "unit": "GB/s",
         "frac": achieved / peak,
         "traffic": traffic,
-        "traffic_source": (capture["source"] if capture else "null: no ncu capture of this build's kernel sources "
+        "traffic_source": (capture["source"] if capture else "null: no ncu capture of the current kernel sources "
                            "is committed"),
         "algorithmic_bytes_per_launch": dom_bytes,
         "ms_per_launch": dom_ms,

@@ -22,13 +22,13 @@ def _tree(tmp_path, digest):
 
 def test_capture_used_only_for_the_sources_it_was_taken_of(tmp_path, monkeypatch):
     monkeypatch.setattr(bench, "ROOT", str(_tree(tmp_path, "0" * 64)))
-    assert bench._capture_of_this_build() is None
+    assert bench._capture_of_current_sources() is None
 
 
 def test_capture_of_the_current_sources_is_used(tmp_path, monkeypatch):
     digest = bench.kernel_source_digest()  # of the repository's flowx_gb300/csrc
     monkeypatch.setattr(bench, "ROOT", str(_tree(tmp_path, digest)))
-    rec = bench._capture_of_this_build()
+    rec = bench._capture_of_current_sources()
     assert rec["bytes_per_launch"]["lambda"] == 123
     assert rec["warp_instructions_per_launch"]["lambda"] == 456
     assert "test capture" in rec["source"]
@@ -36,4 +36,4 @@ def test_capture_of_the_current_sources_is_used(tmp_path, monkeypatch):
 
 def test_missing_summary_gives_none(tmp_path, monkeypatch):
     monkeypatch.setattr(bench, "ROOT", str(tmp_path))
-    assert bench._capture_of_this_build() is None
+    assert bench._capture_of_current_sources() is None
