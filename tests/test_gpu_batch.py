@@ -48,26 +48,37 @@ def test_batch_equals_scenes_stepped_alone(graph):
 def test_batch_beyond_the_constant_segment_table():
     """A batch reads its scenes' parameters from its slice of a constant-memory
     copy of the segment table (128 entries per device), or from the device
-    table when the slice does not fit. 130 scenes take the device table; the
-    same scenes as two batches of 65, one after the other, each take a slice.
-    The substeps are the same bit for bit (the re-associated arithmetic)."""
+    table when no slice is free. 130 scenes take the device table; the same
+    scenes as two batches of 65 alive at once take a slice (the first) and the
+    device table (the second: 63 entries are left); the second again, after
+    the first has closed, takes the slice the first released. Every one of
+    these substeps is the same bit for bit (the re-associated arithmetic)."""
     from flowx_gb300.batch import Batch
 
     sc = scenes.batched_scenes(count=130, seed=7, n_range=(200, 600))
     nsub = 2
-    with Batch(sc) as b:
+    names = ("positions", "velocities", "lambda")
+
+    def run(b):
         b.build_grid()
         b.step(4, nsub)
-        want = {name: b.read(name) for name in ("positions", "velocities", "lambda")}
-    lo = 0
-    for part in (sc[:65], sc[65:]):
-        n = sum(x.n for x in part)
-        with Batch(part) as b:
-            b.build_grid()
-            b.step(4, nsub)
-            for name, arr in want.items():
-                np.testing.assert_array_equal(b.read(name), arr[lo:lo + n], err_msg=name)
-        lo += n
+        return {name: b.read(name) for name in names}
+
+    with Batch(sc) as b:
+        want = run(b)
+    n1 = sum(x.n for x in sc[:65])
+    first, second = sc[:65], sc[65:]
+
+    def check(got, lo, tag):
+        for name in names:
+            np.testing.assert_array_equal(got[name], want[name][lo:lo + len(got[name])], err_msg=f"{tag} {name}")
+
+    with Batch(first) as b1:
+        check(run(b1), 0, "first (slice)")
+        with Batch(second) as b2:
+            check(run(b2), n1, "second (table full)")
+    with Batch(second) as b3:
+        check(run(b3), n1, "second (released slice)")
 
 
 def test_batch_scene_matches_oracle():
