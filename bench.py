@@ -850,6 +850,8 @@ def main():
     ap.add_argument("--exact", action="store_true", help="with --case: the reference's float expressions")
     ap.add_argument("--mesh-collider", action="store_true",
                     help="with --case: voxelise the large scene's falling sphere from its triangle mesh every frame")
+    ap.add_argument("--aux", action="store_true",
+                    help="with --case: drive the kernels outside the steady-state substep once each (run_case_aux)")
     ap.add_argument("--surface", action="store_true",
                     help="with --case: then the frame's surface twice (splat and marching cubes)")
     args = ap.parse_args()
@@ -857,6 +859,8 @@ def main():
         print("bench.py: --warmup below 3 is raised to 3", file=sys.stderr)
         args.warmup = 3
     if args.case:
+        if args.aux:
+            return run_case_aux(args)
         return run_case_adjoint(args) if args.workload == "inverse" else run_case(args)
     if args.workload == "inverse":
         raise SystemExit("--workload inverse is a --case workload; the bench line reports it under 'adjoint'")
@@ -904,6 +908,72 @@ def run_case(args):
     ok = bool(np.isfinite(sol.read("positions")).all())
     sol.close()
     print(json.dumps({"case": scene.name, "frames": args.warmup, "finite": ok}))
+    return 0 if ok else 1
+
+
+def run_case_aux(args):
+    """Untimed run for a DRAM capture of the kernels outside the steady-state
+    substep, each driven once on the 4M-particle workload: the per-pass API
+    (normal, predict, lambda with its quads fill, delta, apply, velocity, XSPH,
+    finalize), downloads and a keys write with their layout conversions, a
+    substep with no Jacobi iteration, the reference's grid order, then the
+    allocation-free grid build at its largest size (65,536 particles) and one
+    3-substep forward and adjoint of the differentiable problem."""
+    import ctypes
+
+    import torch
+
+    from flowx_gb300 import _lib, scenes
+    from flowx_gb300.adjoint import InverseProblem
+    from flowx_gb300.sph import Solver
+
+    torch.cuda.set_device(0)
+    sc = scenes.large()
+    cfg, dt, dims = sc.config, sc.dt, sc.collider_dims
+    with Solver(cfg, sc.positions, sc.velocities, exact=True, max_collider_voxels=int(np.prod(dims))) as s:
+        s.voxelize(sc.primitives_at(3), dims, sc.collider_voxel)
+        s._build_grid(0.0)
+        for name in ("normal", "predict"):
+            s.run_pass(name, dt)
+        s._build_grid(dt)
+        for name in ("lambda", "delta", "apply_delta", "velocity", "xsph", "finalize"):
+            s.run_pass(name, dt)
+        s.read("lambda")
+        s.write("keys", s.read("keys", cfg.sorted_count))
+        rc = s.lib.flowx_substep(s._ctx, ctypes.byref(s.push(dt)), 0)
+        if rc != _lib.FLOWX_OK:
+            raise RuntimeError(f"flowx_substep with no iteration: {rc}")
+        ok = bool(np.isfinite(s.read("positions")).all())
+    with Solver(cfg, sc.positions, sc.velocities, exact=True, reference_order=True) as s:
+        s._build_grid(0.0)
+        s._substep(dt)
+        ok = ok and bool(np.isfinite(s.read("positions")).all())
+    lib = _lib.load()
+    dam = scenes.dam_break()
+    n = 65536
+    rng = np.random.default_rng(1)
+    lo, hi = np.array(dam.config.lo), np.array(dam.config.hi)
+    pts = np.zeros((n, 4), np.float32)
+    pts[:, :3] = lo + rng.random((n, 3)) * (hi - lo)
+    pts[:, 3] = 1.0
+    with Solver(dam.config, dam.positions, dam.velocities) as s:
+        push = s.push(0.0)
+    push.i_layout[0] = n
+    pred = torch.from_numpy(pts).to("cuda:0")
+    keys = torch.zeros((n, 4), dtype=torch.float32, device="cuda:0")
+    start = torch.zeros(dam.config.cell_count, dtype=torch.float32, device="cuda:0")
+    end = torch.zeros(dam.config.cell_count, dtype=torch.float32, device="cuda:0")
+    for _ in range(2):
+        rc = lib.flowx_build_grid_static(pred.data_ptr(), n, ctypes.byref(push), keys.data_ptr(), n,
+                                         start.data_ptr(), end.data_ptr(), None)
+        if rc != _lib.FLOWX_OK:
+            raise RuntimeError(lib.flowx_build_grid_static_error().decode())
+    torch.cuda.synchronize()
+    ip = InverseProblem(scenes.inverse_problem(), substeps=3)
+    control = ip.initial.clone().requires_grad_(True)
+    ip.loss(control).backward()
+    ok = ok and bool(torch.isfinite(control.grad).all())
+    print(json.dumps({"case": "auxiliary kernels", "finite": ok}))
     return 0 if ok else 1
 
 
