@@ -23,8 +23,9 @@ and runs one substep (solver/sph.py:501-514):
 
 States: the seeded lattice with the collider where the benchmark meets it
 (the large scene's sphere at frame 10, a third of it under the free surface),
-and the state the GPU's own FAST run reaches after some frames (moving
-fluid, the sphere inside it, particles pushed out of the collider).
+and the states the GPU's own FAST run reaches after some frames (moving
+fluid, the sphere inside it, particles pushed out of the collider; for the
+large scene also after 60 frames, in the agitated state it keeps).
 """
 
 import numpy as np
@@ -144,6 +145,13 @@ def test_large_after_twelve_frames(large):
     state = _after_frames(large, 12)
     _check_reference_order(large, state, large.collider_grid(12), "large after 12 frames")
     _check(large, state, large.collider_grid(12), "large after 12 frames")
+
+
+def test_large_after_sixty_frames(large):
+    """The agitated state the benchmark runs in (cohesion drives most
+    interior particles to the speed clamp every substep)."""
+    state = _after_frames(large, 60)
+    _check(large, state, large.collider_grid(60), "large after 60 frames")
 
 
 def test_pool_seeded(pool):
