@@ -162,3 +162,10 @@ def test_pool_seeded(pool):
 def test_pool_after_twenty_four_frames(pool):
     state = _after_frames(pool, 24)
     _check(pool, state, pool.collider_grid(0), "pool after 24 frames")
+
+
+def test_pool_after_its_full_run(pool):
+    """The state at the end of the pool's 120-frame run, in both grid orders."""
+    state = _after_frames(pool, 120)
+    _check_reference_order(pool, state, pool.collider_grid(0), "pool after 120 frames")
+    _check(pool, state, pool.collider_grid(0), "pool after 120 frames")
