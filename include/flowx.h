@@ -288,7 +288,11 @@ int64_t flowx_launch_count(void);
 /* Install the scenes, one push block each (particle count, grid, parameters,
  * collider dims / voxel). The counts must sum to the context's particle
  * count. Single-scene entry points (flowx_substep, flowx_step, ...) are then
- * refused; use the batch ones. */
+ * refused; use the batch ones. The kernels read the scenes' parameters from
+ * a 128-entry constant-memory table per device, which the process's batches
+ * share (a slice each, first come, first served, returned on destroy); a
+ * batch that finds no room reads them from device memory instead: the same
+ * results, a few percent slower. */
 int flowx_batch_set_scenes(flowx_ctx *ctx, const flowx_push *pushes, int nscenes);
 
 /* Where a scene lives in the concatenated arrays. */
