@@ -681,6 +681,7 @@ def run_flowx(args):
     capture = _capture_of_current_sources()
     traffic = capture.get("bytes_per_launch", {}).get(dominant) if capture else None
     warp_inst = capture.get("warp_instructions_per_launch", {}).get(dominant) if capture else None
+    lanes = capture.get("active_lanes_per_warp_instruction", {}).get(dominant) if capture else None
     roofline = {
         "bound": "hbm",
         "kernel": dominant,
@@ -791,7 +792,8 @@ def run_flowx(args):
             issue_roofline = {"kernel": dominant, "warp_instructions_per_launch": warp_inst,
                               "ms_per_launch": dom_ms, "achieved": achieved_issue, "peak": peak_issue,
                               "unit": "warp-instructions/s", "frac": achieved_issue / peak_issue,
-                              "peak_basis": f"4 x {sms} SMs x {clock_summary['sm_max_mhz']:.0f} MHz"}
+                              "peak_basis": f"4 x {sms} SMs x {clock_summary['sm_max_mhz']:.0f} MHz",
+                              "active_lanes_per_instruction": lanes}
         line = {
             "metric": METRIC,
             "value": value,
