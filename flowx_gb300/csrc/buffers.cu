@@ -457,18 +457,21 @@ int Ctx::profile_substeps(int iterations, int substeps, float *ms, int32_t *laun
       launches[K_BITONIC] += launched;
       g_launches += launched;
     } else {
-      timed(K_SCATTER, 1, [&] { launch_scatter(d, c->stream); });
+      timed(K_SCATTER, 1, [&] { launch_scatter(d, c->stream, d.x_order != 0); });
       timed(K_CELL_SORT_SMALL, 2, [&] { launch_cell_sort(d, c->stream); });
     }
     timed(K_PERMUTE_STEP, 1, [&] { launch_permute_step(d, d.pred_a, d.normal_alt, c->stream); });
     float4 *q_in = d.pred_a, *q_out = d.pred_b;
     for (int it = 0; it < iterations; ++it) {
+      if (d.trim) timed(K_ROW_BOUNDS, 1, [&] { launch_row_bounds(d, q_in, c->stream); });
       timed(K_LAMBDA, 1, [&] { launch_lambda_f(d, q_in, exact, c->stream); });
       const bool last = it == iterations - 1;
       timed(K_DELTA_APPLY, 1, [&] { launch_delta_apply_f(d, q_in, q_out, exact, last, c->stream); });
       std::swap(q_in, q_out);
+      if (d.trim) std::swap(c->d.quads, c->d.quads_alt);  // d aliases c->d
     }
     if (iterations == 0) launch_xsph_inputs(d, q_in, exact, c->stream);
+    if (d.trim) timed(K_ROW_BOUNDS, 1, [&] { launch_row_bounds(d, q_in, c->stream); });
     timed(K_XSPH_FINALIZE, 1, [&] {
       launch_xsph_finalize_f(d, q_in, d.pos, (c->flags & FLOWX_FLAG_KEEP_DELTA) != 0, exact, sigma,
                              c->stream);

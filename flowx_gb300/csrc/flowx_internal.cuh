@@ -54,6 +54,7 @@ constexpr int kMaxRankSortCell = 4096;
 struct SegParams {
   int p_begin, p_count;        // slots [p_begin, p_begin + p_count)
   int c_begin, c_count;        // cells [c_begin, c_begin + c_count)
+  int r_begin;                 // first x-row (the nx cells of one (y, z)) in the context's numbering
   int nx, ny, nz;              // i_grid.xyz
   float lox, loy, loz, cell;   // f_lo
   float hix, hiy, hiz, radius; // f_hi (solver passes) / surface lo (splat)
@@ -100,6 +101,7 @@ enum KernelId {
   K_SCATTER_IDS,
   K_VOXELIZE,
   K_BITONIC,
+  K_ROW_BOUNDS,
   K_COUNT
 };
 
@@ -161,6 +163,19 @@ struct DeviceState {
   float4 *xv;               // per slot: velocity (pred - pos) / dt and max(rho, 1e-6) entering XSPH
   SlotQuad *quads;          // ceil(n / 4) groups: the predicted positions the next lambda or
                             // XSPH pass filters (written by permute_step, delta_apply, fill_quads)
+  SlotQuad *quads_alt;      // trimmed walk (trim): delta_apply writes the next quads here, since
+                            // its own walk reads d.quads; the runtime swaps the two after it
+  // Candidate trimming of those passes (row_bounds, before each of them):
+  float2 *quad_bounds;      // per quad g: (.x) the largest x of the slots of its x-row from the
+                            // x-row's first slot to slot 4g + 3, (.y) the smallest x from slot 4g
+                            // to the x-row's last slot
+  float4 *row_yz;           // per cell: y and z bounds (ymin, ymax, zmin, zmax) of the particles of
+                            // the cells x - 1, x, x + 1 of its x-row
+  uint32_t *sort_x;         // per old slot during a fused grid build: its predicted x as an
+                            // order-preserving integer (x_order)
+  int xrows;                // x-rows of all segments
+  int trim;                 // lambda and XSPH trim their rows (quad_bounds, row_yz are maintained)
+  int x_order;              // the fused grid build orders each cell by predicted x, not by id
   unsigned long long *bitonic;  // FLOWX_FLAG_REFERENCE_ORDER: the (cell << 32 | id) array the
                                 // reference's sort network orders (bitonic_n entries)
   uint32_t *bitonic_inv;    // per particle id: its slot before the build
@@ -320,7 +335,9 @@ __device__ __forceinline__ int3 collider_coord(const SegParams &s, float px, flo
 void launch_predict_key(const DeviceState &d, const float4 *normal_in, cudaStream_t st);
 void launch_key_only(const DeviceState &d, const float4 *pred, cudaStream_t st);
 void launch_scan(const DeviceState &d, cudaStream_t st);
-void launch_scatter(const DeviceState &d, cudaStream_t st);
+// x_order: (predicted x, old slot) pairs from d.sort_x, the ids kept in
+// d.rank_tmp for permute_step; else (id, old slot) pairs.
+void launch_scatter(const DeviceState &d, cudaStream_t st, bool x_order = false);
 void launch_cell_sort(const DeviceState &d, cudaStream_t st);
 // FLOWX_FLAG_REFERENCE_ORDER in place of scatter + cell_sort: d.pairs from the
 // reference's bitonic network over the keys predict_key / key_only left
@@ -335,6 +352,9 @@ void launch_lambda(const DeviceState &d, const float4 *pred, cudaStream_t st);
 // d.quads <- pred (the per-pass API's lambda, whose input was not written
 // by permute_step or delta_apply)
 void launch_fill_quads(const DeviceState &d, const float4 *pred, cudaStream_t st);
+// quad_bounds and row_yz from pred, for a lambda or XSPH pass over pred that
+// trims its rows (d.trim)
+void launch_row_bounds(const DeviceState &d, const float4 *pred, cudaStream_t st);
 // fused substep (exact = the reference's expressions, else re-associated).
 // lambda and xsph_finalize filter candidates from d.quads, which must hold
 // `pred`: permute_step and delta_apply leave there what they write.

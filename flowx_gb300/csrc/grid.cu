@@ -10,7 +10,7 @@
 //                     counters are re-zeroed on the way, cells holding more
 //                     than kSmallCellSort particles are listed;
 //   3. scatter      - (id, old slot) to offset[key] + rank, in a scratch copy;
-//   4. cell_sort    - order each cell by particle id: every pair of a cell of
+//   4. cell_sort    - order each cell by its pairs: every pair of a cell of
 //                     at most kSmallCellSort particles counts the smaller pairs
 //                     of its cell and moves to that rank (thread per slot), a
 //                     block ranks each listed large cell; the result is the
@@ -19,7 +19,10 @@
 //
 // The sorted key column, the [start, end) of every cell and each cell's
 // membership equal the reference's; within a cell the reference's bitonic
-// network leaves an arbitrary order, this leaves ascending ids.
+// network leaves an arbitrary order, this leaves ascending ids. The fused
+// substep's build in the re-associated arithmetic (x_order) orders each cell
+// by predicted x instead (ties by old slot), so that the slots of a stencil row
+// run in x and the neighbour passes can trim a row to the particle's reach.
 #include "pbf_math.cuh"
 
 namespace flowx {
@@ -42,8 +45,17 @@ __device__ __forceinline__ void count_key(uint32_t *counts, uint32_t key, bool a
   rank = base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
 }
 
+// Order-preserving integer of a float (negative values reversed below the
+// positive ones; NaN above +inf).
+__device__ __forceinline__ uint32_t ordered_bits(float x)
+{
+  const uint32_t u = __float_as_uint(x);
+  return u ^ ((u >> 31) ? 0xffffffffu : 0x80000000u);
+}
+
 // Fused substep: pos/vel/normal -> key, rank (the predicted position itself is
-// recomputed by the permute, which is cheaper than storing and re-reading it).
+// recomputed by the permute, which is cheaper than storing and re-reading it;
+// x_order keeps its x for the scatter).
 template <int SEG>
 __global__ void k_predict_key(DeviceState d, const float4 *__restrict__ normal_in)
 {
@@ -59,6 +71,7 @@ __global__ void k_predict_key(DeviceState d, const float4 *__restrict__ normal_i
     predict_particle(s, p, v, n, vo, q);
     key = (uint32_t)(s.c_begin + cell_index(s, cell_coord(s, q.x, q.y, q.z)));
     d.key_tmp[k] = key;
+    if (d.x_order) d.sort_x[k] = ordered_bits(q.x);
   }
   uint32_t rank = 0;
   count_key(d.counts, key, active, rank);
@@ -216,25 +229,37 @@ void launch_scan(const DeviceState &d, cudaStream_t st)
 }
 
 // ---- 3. scatter ---------------------------------------------------------
+// X_ORDER: the pair leads with the predicted x (d.sort_x) and the id waits in
+// d.rank_tmp[k] (this thread's rank, just read) for permute_step.
+template <bool X_ORDER>
 __global__ void k_scatter(DeviceState d)
 {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= d.n) return;
   const uint32_t key = d.key_tmp[k];
   const uint32_t slot = d.offsets[key] + d.rank_tmp[k];
-  d.pairs_tmp[slot] = ((unsigned long long)d.ids[k] << 32) | (unsigned long long)(uint32_t)k;
+  const uint32_t id = d.ids[k];
+  if (X_ORDER) {
+    d.pairs_tmp[slot] = ((unsigned long long)d.sort_x[k] << 32) | (unsigned long long)(uint32_t)k;
+    d.rank_tmp[k] = id;
+  } else {
+    d.pairs_tmp[slot] = ((unsigned long long)id << 32) | (unsigned long long)(uint32_t)k;
+  }
 }
 
-void launch_scatter(const DeviceState &d, cudaStream_t st)
+void launch_scatter(const DeviceState &d, cudaStream_t st, bool x_order)
 {
-  const int b = FLOWX_BLOCK(d, K_SCATTER, 256, k_scatter);
-  if (d.n > 0) k_scatter<<<grid_for(d.n, b), b, 0, st>>>(d);
+  const int b = FLOWX_BLOCK(d, K_SCATTER, 256, x_order ? (const void *)k_scatter<true> : (const void *)k_scatter<false>);
+  if (d.n <= 0) return;
+  if (x_order) k_scatter<true><<<grid_for(d.n, b), b, 0, st>>>(d);
+  else k_scatter<false><<<grid_for(d.n, b), b, 0, st>>>(d);
 }
 
-// ---- 4. order each cell by id -------------------------------------------
-// Cells of at most kSmallCellSort particles: each slot's (id, old slot) pair
-// counts the smaller pairs of its cell in the scatter's copy (ids are unique,
-// so the counts are a permutation of the cell's ranks) and moves there. A
+// ---- 4. order each cell by its pairs ---------------------------------------
+// Cells of at most kSmallCellSort particles: each slot's (id or x, old slot)
+// pair counts the smaller pairs of its cell in the scatter's copy (old slots
+// are unique, so the counts are a permutation of the cell's ranks) and moves
+// there. A
 // warp's slots mostly share one cell, whose pairs its loads then share.
 __global__ void k_cell_rank(DeviceState d)
 {
@@ -396,7 +421,8 @@ int launch_reference_order(const DeviceState &d, cudaStream_t st)
 // Fused substep: new slot k takes old slot s. Positions are copied, the
 // predicted position recomputed from (pos, vel, normal) exactly as predict did,
 // the substep's normal (computed into scratch in the old order) moved to the
-// new slot, and the slot's key and id recorded. Velocity and lambda need no
+// new slot, and the slot's key and id recorded (x_order: the id the scatter
+// left in rank_tmp). Velocity and lambda need no
 // copy: the rest of the substep rewrites them before reading.
 template <int SEG>
 __global__ void k_permute_step(DeviceState d, float4 *__restrict__ pred_out, const float4 *__restrict__ normal_in)
@@ -415,7 +441,7 @@ __global__ void k_permute_step(DeviceState d, float4 *__restrict__ pred_out, con
   d.pos_alt[k] = p;
   pred_out[k] = make_float4(q.x, q.y, q.z, 1.0f);
   store_quad(d.quads, k, q.x, q.y, q.z);
-  d.ids[k] = (uint32_t)(pr >> 32);
+  d.ids[k] = d.x_order ? d.rank_tmp[s] : (uint32_t)(pr >> 32);
   d.keys[k] = d.key_tmp[s];
 }
 

@@ -155,6 +155,14 @@ __device__ __forceinline__ float2 pair_r2_x2(float2 qx, float2 qy, float2 qz, fl
   return __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
 }
 
+// Bounds of the current positions that let phase 1 skip candidates beyond
+// reach (row_bounds in pbf.cu maintains them for the positions in the quads).
+struct RowTrim {
+  const float2 *__restrict__ quad_bounds;  // per quad: x-row prefix max of x at its last slot,
+                                           // x-row suffix min of x at its first slot
+  const float4 *__restrict__ row_yz;       // per cell: y, z bounds of its x-row neighbourhood
+};
+
 // build_row_masks over the slot quads: the same masks, four candidates per
 // three 16-byte loads. A row [ra, rb) is covered by the quads ra/4 .. (rb-1)/4;
 // their accept bits are assembled in order, the ra % 4 bits of slots before
@@ -224,13 +232,106 @@ __device__ __forceinline__ bool build_row_masks_quads(const SegParams &s, const 
   return true;
 }
 
+// The walk for cells coarser than the reach (rows of more than 64 slots):
+// each stencil row's run trimmed to the particle's reach, then tested and
+// visited sixteen quads at a time (a 64-bit mask in registers per chunk,
+// its set bits visited at once), rows in order, slots ascending. The trim:
+//   every candidate of the row lies within the y, z bounds of the row's
+//   cells, so its squared distance is at least g^2, the squared y-z gap from
+//   p to those bounds, and a row with g^2 beyond reach has no candidate;
+//   otherwise a candidate can only be within reach when |x - p.x| < rx =
+//   sqrt(reach^2 - g^2): the leading quads whose slots all lie left of
+//   p.x - rx (the x-row's running maximum of x at their last slot says so)
+//   and the trailing ones whose slots all lie right of p.x + rx (the running
+//   minimum at their first slot) hold none.
+// reach^2 is the test's lim2 widened by 2^-10 and the x window by 2^-20
+// (|p.x| + rx), far above the rounding of the test and of these bounds, so
+// every candidate the test accepts is visited, in the untrimmed walk's order.
+// (A NaN coordinate of p makes every test reject, and its window comparisons
+// fail, trimming nothing.) Slots in any order within a cell are handled; the
+// x-ordered cells of the re-associated build make the trimmed runs short. A
+// row above the reference's MAX_CELL_SCAN is walked cell by cell with the
+// cap, as for_each_within_rows does.
+template <bool EXACT, class F>
+__device__ __forceinline__ void for_each_within_trimmed(const SegParams &s, const uint32_t *__restrict__ off,
+                                                        const SlotQuad *__restrict__ quads, RowTrim trim, float4 p,
+                                                        float lim2, int3 base, F &&f)
+{
+  const int x0 = max(base.x - 1, 0), x1 = min(base.x + 1, s.nx - 1);
+  const float2 npx = make_float2(-p.x, -p.x), npy = make_float2(-p.y, -p.y), npz = make_float2(-p.z, -p.z);
+  const float reach2 = lim2 * (1.0f + 0x1p-10f);
+#pragma unroll 1
+  for (int r = 0; r < kRows; ++r) {
+    const int z = base.z + (r / 3) - 1;
+    const int y = base.y + (r % 3) - 1;
+    if (z < 0 || z >= s.nz || y < 0 || y >= s.ny) continue;
+    const int row = s.c_begin + (z * s.ny + y) * s.nx;
+    const uint32_t ra = __ldg(&off[row + x0]);
+    const uint32_t rb = __ldg(&off[row + x1 + 1]);
+    if (rb <= ra) continue;
+    if (rb - ra > (uint32_t)kMaxCellScan) {
+#pragma unroll 1
+      for (int x = x0; x <= x1; ++x) {
+        const uint32_t cs = __ldg(&off[row + x]);
+        uint32_t ce = __ldg(&off[row + x + 1]);
+        if (ce - cs > (uint32_t)kMaxCellScan) ce = cs + kMaxCellScan;
+#pragma unroll 1
+        for (uint32_t k = cs; k < ce; ++k) f((int)k, false);
+      }
+      continue;
+    }
+    const float4 yz = __ldg(&trim.row_yz[row + base.x]);
+    const float gy = fmaxf(fmaxf(yz.x - p.y, p.y - yz.y), 0.0f);
+    const float gz = fmaxf(fmaxf(yz.z - p.z, p.z - yz.w), 0.0f);
+    const float rx2 = reach2 - (gy * gy + gz * gz);
+    if (!(rx2 > 0.0f)) continue;  // the whole row beyond reach
+    uint32_t t0 = ra >> 2, t1 = (rb + 3u) >> 2;
+    const float rx = sqrtf(rx2);
+    const float tol = (fabsf(p.x) + rx) * 0x1p-20f;
+    const float xlo = p.x - rx - tol, xhi = p.x + rx + tol;
+#pragma unroll 1
+    while (t0 < t1 && 4u * t0 + 3u < rb && __ldg(&trim.quad_bounds[t0].x) < xlo) ++t0;
+#pragma unroll 1
+    while (t1 > t0 && 4u * (t1 - 1u) >= ra && __ldg(&trim.quad_bounds[t1 - 1u].y) > xhi) --t1;
+#pragma unroll 1
+    for (uint32_t c0 = t0; c0 < t1; c0 += 16u) {
+      const uint32_t c1 = min(c0 + 16u, t1), nq = c1 - c0;
+      // each quad enters a 64-bit window (hi:lo) from the top; after the
+      // last, slot 4 c0 + s sits at bit 64 - 4 nq + s
+      uint32_t lo = 0u, hi = 0u;
+#pragma unroll 1
+      for (uint32_t g = c0; g < c1; ++g) {
+        const float4 X = __ldg(&quads[g].x), Y = __ldg(&quads[g].y), Z = __ldg(&quads[g].z);
+        const float2 a = pair_r2_x2<EXACT>(make_float2(X.x, X.y), make_float2(Y.x, Y.y), make_float2(Z.x, Z.y),
+                                           npx, npy, npz);
+        const float2 b = pair_r2_x2<EXACT>(make_float2(X.z, X.w), make_float2(Y.z, Y.w), make_float2(Z.z, Z.w),
+                                           npx, npy, npz);
+        const uint32_t nib =
+            (a.x < lim2 ? 1u : 0u) | (a.y < lim2 ? 2u : 0u) | (b.x < lim2 ? 4u : 0u) | (b.y < lim2 ? 8u : 0u);
+        lo = __funnelshift_r(lo, hi, 4);
+        hi = (hi >> 4) | (nib << 28);
+      }
+      unsigned long long m = (((unsigned long long)hi << 32) | lo) >> (64u - 4u * nq);
+      const uint32_t wb = 4u * c0;
+      if (ra > wb) m &= ~((1ull << (ra - wb)) - 1ull);       // slots before the row
+      if (rb - wb < 4u * nq) m &= (1ull << (rb - wb)) - 1ull;  // slots past it
+#pragma unroll 1
+      while (m) {
+        const int t = __ffsll((long long)m) - 1;
+        m &= m - 1ull;
+        f((int)(wb + (uint32_t)t), true);
+      }
+    }
+  }
+}
+
 // Phase 2: every set bit of every row, rows in order, slots ascending; each
 // lane moves to its next row when its current mask runs out.
 template <class F>
 __device__ __forceinline__ void visit_row_masks(const SegParams &s, const uint32_t *__restrict__ off, int3 base,
                                                 const unsigned long long *mine, int stride, F &&f)
 {
-  const int x0 = max(base.x - 1, 0), x1 = min(base.x + 1, s.nx - 1);
+  const int x0 = max(base.x - 1, 0);
   int r = -1;
   unsigned long long m = 0ull;
   uint32_t ra = 0;
@@ -280,11 +381,16 @@ struct MaskRecord {
 
 // for_each_within with phase 1 over the slot quads (quads[k / 4] lane k % 4
 // holding pos[k]).
-template <bool EXACT, class F>
+// WIN: cells coarser than the reach, the trimmed walk (for_each_within_trimmed).
+template <bool EXACT, bool WIN, class F>
 __device__ __forceinline__ void for_each_within(const SegParams &s, const uint32_t *__restrict__ off,
                                                 const float4 *__restrict__ pos, const SlotQuad *__restrict__ quads,
-                                                float4 p, float lim2, int3 base, F &&f)
+                                                RowTrim trim, float4 p, float lim2, int3 base, F &&f)
 {
+  if (WIN) {
+    for_each_within_trimmed<EXACT>(s, off, quads, trim, p, lim2, base, f);
+    return;
+  }
   extern __shared__ unsigned long long row_masks[];
   unsigned long long *mine = row_masks + threadIdx.x;
   if (build_row_masks_quads<EXACT>(s, off, quads, p, lim2, base, mine, blockDim.x))
@@ -295,12 +401,16 @@ __device__ __forceinline__ void for_each_within(const SegParams &s, const uint32
 
 // for_each_within (phase 1 over the slot quads) that also records slot i's
 // masks.
-template <bool EXACT, class F>
+template <bool EXACT, bool WIN, class F>
 __device__ __forceinline__ void for_each_within_recording(const SegParams &s, const uint32_t *__restrict__ off,
                                                           const float4 *__restrict__ pos,
-                                                          const SlotQuad *__restrict__ quads, float4 p, float lim2,
-                                                          int3 base, MaskRecord rec, int i, F &&f)
+                                                          const SlotQuad *__restrict__ quads, RowTrim trim, float4 p,
+                                                          float lim2, int3 base, MaskRecord rec, int i, F &&f)
 {
+  if (WIN) {  // nothing recorded: the delta pass walks its trimmed rows too
+    for_each_within_trimmed<EXACT>(s, off, quads, trim, p, lim2, base, f);
+    return;
+  }
   extern __shared__ unsigned long long row_masks[];
   unsigned long long *mine = row_masks + threadIdx.x;
   const int stride = blockDim.x;
@@ -317,11 +427,17 @@ __device__ __forceinline__ void for_each_within_recording(const SegParams &s, co
 
 // for_each_within from slot i's recorded masks, left by the launch just
 // before on the same stream (same positions, grid and reach): phase 2 only.
-template <bool EXACT, class F>
+// WIN (nothing recorded): the trimmed walk over the same positions' quads.
+template <bool EXACT, bool WIN, class F>
 __device__ __forceinline__ void for_each_within_recorded(const SegParams &s, const uint32_t *__restrict__ off,
-                                                         const float4 *__restrict__ pos, float4 p, float lim2,
-                                                         int3 base, MaskRecord rec, int i, F &&f)
+                                                         const float4 *__restrict__ pos,
+                                                         const SlotQuad *__restrict__ quads, RowTrim trim, float4 p,
+                                                         float lim2, int3 base, MaskRecord rec, int i, F &&f)
 {
+  if (WIN) {
+    for_each_within_trimmed<EXACT>(s, off, quads, trim, p, lim2, base, f);
+    return;
+  }
   extern __shared__ unsigned long long row_masks[];
   unsigned long long *mine = row_masks + threadIdx.x;
   const int stride = blockDim.x;

@@ -6,9 +6,11 @@
 //   normal          sph_normal.glsl                      (if sigma > 0)
 //   predict_key     sph_predict.glsl + sph_grid_key.glsl (grid.cu)
 //   scan/scatter/sort/permute                             (grid.cu)
-//   I x { lambda    sph_lambda.glsl
+//   I x { row_bounds  (the bounds lambda trims its rows with)
+//         lambda    sph_lambda.glsl
 //         delta_apply sph_delta.glsl + sph_apply_delta.glsl, written to the
 //                     other predicted buffer (ping-pong) }
+//   row_bounds
 //   xsph_finalize   sph_velocity.glsl + sph_xsph.glsl + sph_finalize.glsl:
 //                   neighbour velocities are re-derived from (pred - pos)/dt,
 //                   the same expression sph_velocity.glsl stores, and the new
@@ -40,7 +42,7 @@ static inline unsigned grid_for(long long n, int b) { return (unsigned)((n + b -
 // latency than the few registers cost, 1.6% per frame), delta_apply four
 // (32), XSPH five 256-thread blocks (48).
 // sph_lambda.glsl:17-77
-template <bool EXACT, int SEG>
+template <bool EXACT, int SEG, bool WIN>
 __global__ void __launch_bounds__(512, 3) k_lambda_f(DeviceState d, const float4 *__restrict__ pred)
 {
   FLOWX_SLOT_PROLOGUE_SEG
@@ -48,7 +50,8 @@ __global__ void __launch_bounds__(512, 3) k_lambda_f(DeviceState d, const float4
   const int3 base = cell_coord(s, pi.x, pi.y, pi.z);
   LambdaAcc<EXACT> acc;
   const MaskRecord rec{d.row_masks, d.row_wide, d.n};
-  for_each_within_recording<EXACT>(s, d.offsets, pred, d.quads, pi, s.h2, base, rec, i, [&](int k, bool within) {
+  const RowTrim trim{d.quad_bounds, d.row_yz};
+  for_each_within_recording<EXACT, WIN>(s, d.offsets, pred, d.quads, trim, pi, s.h2, base, rec, i, [&](int k, bool within) {
     const float4 pj = __ldg(&pred[k]);
     acc.pair(s, pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, within);
   });
@@ -63,7 +66,7 @@ __global__ void __launch_bounds__(512, 3) k_lambda_f(DeviceState d, const float4
 // in for phase 1; the body keeps its own j != i and r^2 > 1e-12 tests.
 // RECORDED also reads each neighbour's position and lambda from d.plam (one
 // 16-byte load; the lambda pass left them there).
-template <bool EXACT, bool RECORDED>
+template <bool EXACT, bool RECORDED, bool WIN = false>
 __device__ __forceinline__ float3 delta_sum_f(const SegParams &s, const DeviceState &d, const float4 *__restrict__ pred,
                                               int i, float4 pi)
 {
@@ -81,8 +84,8 @@ __device__ __forceinline__ float3 delta_sum_f(const SegParams &s, const DeviceSt
     delta_pair<EXACT>(s, lambda_i, RECORDED ? pj.w : __ldg(&d.lam[k].y), dx, dy, dz, r2, ax, ay, az);
   };
   if (RECORDED)
-    for_each_within_recorded<EXACT>(s, d.offsets, pred, pi, h2, base, MaskRecord{d.row_masks, d.row_wide, d.n},
-                                    i, body);
+    for_each_within_recorded<EXACT, WIN>(s, d.offsets, pred, d.quads, RowTrim{d.quad_bounds, d.row_yz}, pi, h2,
+                                         base, MaskRecord{d.row_masks, d.row_wide, d.n}, i, body);
   else
     for_each_within<EXACT>(s, d.offsets, pred, pi, h2, base, body);
   return make_float3(ax, ay, az);
@@ -123,17 +126,17 @@ __device__ __forceinline__ void normal_terms(const SegParams &s, float rho_j, fl
 // gathers are latency-bound, and the full 64 resident warps hide more of them
 // (0.726 -> 0.688 ms per launch on the 4M-particle workload); the reference
 // form would spill at 32 and keeps three.
-template <bool EXACT, int SEG>
+template <bool EXACT, int SEG, bool WIN>
 __global__ void __launch_bounds__(512, EXACT ? 3 : 4) k_delta_apply_f(DeviceState d, const float4 *__restrict__ pred_in,
                                                        float4 *__restrict__ pred_out, int last)
 {
   FLOWX_SLOT_PROLOGUE_SEG
   const float4 pi = pred_in[i];
-  const float3 a = delta_sum_f<EXACT, true>(s, d, pred_in, i, pi);
+  const float3 a = delta_sum_f<EXACT, true, WIN>(s, d, pred_in, i, pi);
   const float rest = s.rest;
   const float4 q = make_float4(pi.x + a.x / rest, pi.y + a.y / rest, pi.z + a.z / rest, 1.0f);
   pred_out[i] = q;
-  store_quad(d.quads, i, q.x, q.y, q.z);
+  store_quad(WIN ? d.quads_alt : d.quads, i, q.x, q.y, q.z);
   if (last) d.xv[i] = xsph_input<EXACT>(s, d, i, q);
 }
 
@@ -152,6 +155,102 @@ __global__ void k_fill_quads(DeviceState d, const float4 *__restrict__ pred)
   store_quad(d.quads, i, q.x, q.y, q.z);
 }
 
+// The bounds the trimmed phase 1 of lambda and XSPH reads (RowTrim in
+// neighbour.cuh), from the positions those passes test. One warp per x-row
+// (the nx cells of one (y, z), whose slots are one contiguous run):
+//  * per cell, the y and z bounds of the particles of its cells x - 1, x,
+//    x + 1 (thirty cells per step, lanes 0 and 31 holding the neighbours
+//    either side);
+//  * along the x-row's slots, the running maximum of x from the first slot
+//    and the running minimum from the last, kept at the last and the first
+//    slot of each quad (slot 4g + 3 and 4g). A quad that straddles two x-rows
+//    takes each value from the x-row that owns that slot; phase 1 reads a
+//    quad's value only when that slot lies in the row it walks.
+// fminf / fmaxf skip NaN coordinates, whose candidates every test rejects.
+constexpr int kRowBoundsBlock = 256;
+
+__global__ void __launch_bounds__(kRowBoundsBlock) k_row_bounds(DeviceState d, const float4 *__restrict__ pred)
+{
+  const int w = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (w >= d.xrows) return;  // whole warps
+  int sg = 0;
+  if (d.nseg > 1) {  // the last segment whose first x-row is <= w
+    int lo = 0, hi = d.nseg - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (d.segs[mid].r_begin <= w) lo = mid; else hi = mid - 1;
+    }
+    sg = lo;
+  }
+  const SegParams &s = d.segs[sg];
+  const int row = s.c_begin + (w - s.r_begin) * s.nx;
+  const uint32_t *__restrict__ off = d.offsets;
+  const unsigned full = 0xffffffffu;
+  const float inf = __int_as_float(0x7f800000);
+#pragma unroll 1
+  for (int c0 = 0; c0 < s.nx; c0 += 30) {
+    const int x = c0 - 1 + lane;
+    float ylo = inf, yhi = -inf, zlo = inf, zhi = -inf;
+    if (x >= 0 && x < s.nx) {
+      const uint32_t a = __ldg(&off[row + x]), b = __ldg(&off[row + x + 1]);
+#pragma unroll 1
+      for (uint32_t k = a; k < b; ++k) {
+        const float4 q = __ldg(&pred[k]);
+        ylo = fminf(ylo, q.y);
+        yhi = fmaxf(yhi, q.y);
+        zlo = fminf(zlo, q.z);
+        zhi = fmaxf(zhi, q.z);
+      }
+    }
+    const float ylo_l = __shfl_up_sync(full, ylo, 1), ylo_r = __shfl_down_sync(full, ylo, 1);
+    const float yhi_l = __shfl_up_sync(full, yhi, 1), yhi_r = __shfl_down_sync(full, yhi, 1);
+    const float zlo_l = __shfl_up_sync(full, zlo, 1), zlo_r = __shfl_down_sync(full, zlo, 1);
+    const float zhi_l = __shfl_up_sync(full, zhi, 1), zhi_r = __shfl_down_sync(full, zhi, 1);
+    if (lane >= 1 && lane <= 30 && x < s.nx)
+      d.row_yz[row + x] = make_float4(fminf(ylo, fminf(ylo_l, ylo_r)), fmaxf(yhi, fmaxf(yhi_l, yhi_r)),
+                                      fminf(zlo, fminf(zlo_l, zlo_r)), fmaxf(zhi, fmaxf(zhi_l, zhi_r)));
+  }
+  const uint32_t A = __ldg(&off[row]), B = __ldg(&off[row + s.nx]);
+  float carry = -inf;
+#pragma unroll 1
+  for (uint32_t b0 = A; b0 < B; b0 += 32u) {
+    const uint32_t k = b0 + (uint32_t)lane;
+    float v = k < B ? __ldg(&pred[k]).x : -inf;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const float t = __shfl_up_sync(full, v, o);
+      if (lane >= o) v = fmaxf(v, t);
+    }
+    v = fmaxf(v, carry);
+    carry = __shfl_sync(full, v, 31);
+    if (k < B && (k & 3u) == 3u) d.quad_bounds[k >> 2].x = v;
+  }
+  carry = inf;
+#pragma unroll 1
+  for (uint32_t t0 = 0; t0 < B - A; t0 += 32u) {
+    const uint32_t t = t0 + (uint32_t)lane;  // slots from the x-row's last
+    const bool in = t < B - A;
+    const uint32_t k = B - 1u - t;
+    float v = in ? __ldg(&pred[k]).x : inf;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const float u = __shfl_up_sync(full, v, o);
+      if (lane >= o) v = fminf(v, u);
+    }
+    v = fminf(v, carry);
+    carry = __shfl_sync(full, v, 31);
+    if (in && (k & 3u) == 0u) d.quad_bounds[k >> 2].y = v;
+  }
+}
+
+void launch_row_bounds(const DeviceState &d, const float4 *pred, cudaStream_t st)
+{
+  if (d.n <= 0 || d.xrows <= 0) return;
+  const int warps = kRowBoundsBlock / 32;
+  k_row_bounds<<<grid_for(d.xrows, warps), kRowBoundsBlock, 0, st>>>(d, pred);
+}
+
 // sph_xsph.glsl:35-81: c * sum (m / rho_j) (v_j - v_i) W(r), neighbour
 // velocities from velj(k, pred_k). QUADS: d.quads holds pred (the fused
 // substep), so phase 1 reads the quads. NORMALS (slots whose segment has
@@ -161,7 +260,7 @@ __global__ void k_fill_quads(DeviceState d, const float4 *__restrict__ pred)
 // them - and leaves the result in *normal_out.
 // The fused pass (QUADS) takes each neighbour's velocity and density from
 // d.xv, left by the last delta_apply.
-template <bool EXACT, bool QUADS, bool NORMALS, class VelJ>
+template <bool EXACT, bool QUADS, bool NORMALS, bool WIN = false, class VelJ>
 __device__ __forceinline__ float3 xsph_sum_f(const SegParams &s, const DeviceState &d, const float4 *__restrict__ pred,
                                              int i, float4 q, float3 vi, VelJ &&velj, float4 *normal_out = nullptr)
 {
@@ -202,7 +301,7 @@ __device__ __forceinline__ float3 xsph_sum_f(const SegParams &s, const DeviceSta
     if (normals) normal_terms<EXACT>(s, rho_j, r2, dx, dy, dz, nx, ny, nz, lap);  // sph_normal.glsl's body
   };
   if (QUADS)
-    for_each_within<EXACT>(s, d.offsets, pred, d.quads, q, h2, base, body);
+    for_each_within<EXACT, WIN>(s, d.offsets, pred, d.quads, RowTrim{d.quad_bounds, d.row_yz}, q, h2, base, body);
   else
     for_each_within<EXACT>(s, d.offsets, pred, q, h2, base, body);
   if (normals) {
@@ -219,7 +318,7 @@ __device__ __forceinline__ float3 xsph_sum_f(const SegParams &s, const DeviceSta
 // of this grid, which the next substep's permute maps to its own). Bounded to
 // five 256-thread blocks per SM (48 registers): with both bodies it spills at
 // 40 (1.68 -> 1.63 ms per launch on the 4M-particle workload).
-template <bool EXACT, bool NORMALS, int SEG>
+template <bool EXACT, bool NORMALS, int SEG, bool WIN>
 __global__ void __launch_bounds__(256, 5) k_xsph_finalize_f(DeviceState d, const float4 *__restrict__ pred,
                                                          float4 *__restrict__ pos_out, int keep_delta)
 {
@@ -227,7 +326,7 @@ __global__ void __launch_bounds__(256, 5) k_xsph_finalize_f(DeviceState d, const
   const float4 q = pred[i];
   const float4 xi = d.xv[i];
   const float3 vi = make_float3(xi.x, xi.y, xi.z);
-  const float3 dv = xsph_sum_f<EXACT, true, NORMALS>(
+  const float3 dv = xsph_sum_f<EXACT, true, NORMALS, WIN>(
       s, d, pred, i, q, vi, [](int, const float4 &) { return make_float3(0.f, 0.f, 0.f); }, d.normal_alt + i);
   float3 v = make_float3(vi.x + dv.x, vi.y + dv.y, vi.z + dv.z);
   float3 p = make_float3(q.x, q.y, q.z);
@@ -263,17 +362,32 @@ __global__ void __launch_bounds__(512, 3) k_normal_f(DeviceState d, const float4
   out[i] = make_float4(nx, ny, nz, curv);
 }
 
+// f(std::bool_constant<WIN>): windowed masks over trimmed rows when the
+// context's cells are coarser than the reach (d.trim), the plain row masks
+// otherwise.
+template <class F>
+static void with_windows(const DeviceState &d, F &&f)
+{
+  if (d.trim)
+    f(std::true_type{});
+  else
+    f(std::false_type{});
+}
+
 void launch_lambda_f(const DeviceState &d, const float4 *pred, bool exact, cudaStream_t st)
 {
   if (d.warp_passes) return launch_lambda_w(d, pred, exact, st);
   if (d.n <= 0) return;
   with_seg_source(d, [&](auto tag) {
-    constexpr int SEG = decltype(tag)::value;
-    const void *fn = exact ? (const void *)k_lambda_f<true, SEG> : (const void *)k_lambda_f<false, SEG>;
-    const int b = FLOWX_BLOCK(d, K_LAMBDA, 128, fn);
-    const unsigned g = grid_for(d.n, b);
-    if (exact) k_lambda_f<true, SEG><<<g, b, row_mask_bytes(b), st>>>(d, pred);
-    else k_lambda_f<false, SEG><<<g, b, row_mask_bytes(b), st>>>(d, pred);
+    with_windows(d, [&](auto wtag) {
+      constexpr int SEG = decltype(tag)::value;
+      constexpr bool WIN = decltype(wtag)::value;
+      const void *fn = exact ? (const void *)k_lambda_f<true, SEG, WIN> : (const void *)k_lambda_f<false, SEG, WIN>;
+      const int b = FLOWX_BLOCK(d, K_LAMBDA, 128, fn);
+      const unsigned g = grid_for(d.n, b);
+      if (exact) k_lambda_f<true, SEG, WIN><<<g, b, row_mask_bytes(b), st>>>(d, pred);
+      else k_lambda_f<false, SEG, WIN><<<g, b, row_mask_bytes(b), st>>>(d, pred);
+    });
   });
 }
 void launch_delta_apply_f(const DeviceState &d, const float4 *pred_in, float4 *pred_out, bool exact, bool last,
@@ -283,12 +397,16 @@ void launch_delta_apply_f(const DeviceState &d, const float4 *pred_in, float4 *p
   if (d.n <= 0) return;
   const int l = last ? 1 : 0;
   with_seg_source(d, [&](auto tag) {
-    constexpr int SEG = decltype(tag)::value;
-    const void *fn = exact ? (const void *)k_delta_apply_f<true, SEG> : (const void *)k_delta_apply_f<false, SEG>;
-    const int b = FLOWX_BLOCK(d, K_DELTA_APPLY, 128, fn);
-    const unsigned g = grid_for(d.n, b);
-    if (exact) k_delta_apply_f<true, SEG><<<g, b, row_mask_bytes(b), st>>>(d, pred_in, pred_out, l);
-    else k_delta_apply_f<false, SEG><<<g, b, row_mask_bytes(b), st>>>(d, pred_in, pred_out, l);
+    with_windows(d, [&](auto wtag) {
+      constexpr int SEG = decltype(tag)::value;
+      constexpr bool WIN = decltype(wtag)::value;
+      const void *fn =
+          exact ? (const void *)k_delta_apply_f<true, SEG, WIN> : (const void *)k_delta_apply_f<false, SEG, WIN>;
+      const int b = FLOWX_BLOCK(d, K_DELTA_APPLY, 128, fn);
+      const unsigned g = grid_for(d.n, b);
+      if (exact) k_delta_apply_f<true, SEG, WIN><<<g, b, row_mask_bytes(b), st>>>(d, pred_in, pred_out, l);
+      else k_delta_apply_f<false, SEG, WIN><<<g, b, row_mask_bytes(b), st>>>(d, pred_in, pred_out, l);
+    });
   });
 }
 void launch_xsph_inputs(const DeviceState &d, const float4 *pred, bool exact, cudaStream_t st)
@@ -302,11 +420,14 @@ static void xsph_finalize_launch(const DeviceState &d, const float4 *pred, float
                                  cudaStream_t st)
 {
   with_seg_source(d, [&](auto tag) {
-    constexpr int SEG = decltype(tag)::value;
-    const void *fn = (const void *)k_xsph_finalize_f<EXACT, NORMALS, SEG>;
-    const int b = FLOWX_BLOCK(d, K_XSPH_FINALIZE, 128, fn);
-    k_xsph_finalize_f<EXACT, NORMALS, SEG><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred, pos_out,
-                                                                                           keep_delta);
+    with_windows(d, [&](auto wtag) {
+      constexpr int SEG = decltype(tag)::value;
+      constexpr bool WIN = decltype(wtag)::value;
+      const void *fn = (const void *)k_xsph_finalize_f<EXACT, NORMALS, SEG, WIN>;
+      const int b = FLOWX_BLOCK(d, K_XSPH_FINALIZE, 128, fn);
+      k_xsph_finalize_f<EXACT, NORMALS, SEG, WIN><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred, pos_out,
+                                                                                                keep_delta);
+    });
   });
 }
 void launch_xsph_finalize_f(const DeviceState &d, const float4 *pred, float4 *pos_out, bool keep_delta, bool exact,
@@ -410,6 +531,7 @@ void launch_fill_quads(const DeviceState &d, const float4 *pred, cudaStream_t st
 void launch_lambda(const DeviceState &d, const float4 *pred, cudaStream_t st)
 {
   launch_fill_quads(d, pred, st);
+  if (d.trim) launch_row_bounds(d, pred, st);
   launch_lambda_f(d, pred, true, st);
 }
 void launch_predict(const DeviceState &d, float4 *pred, cudaStream_t st)

@@ -31,6 +31,7 @@ static const char *kKernelNames[K_COUNT] = {
     "cell_sort_small", "cell_sort_large", "permute_step", "lambda",  "delta_apply",  "xsph_finalize",
     "splat",         "predict",      "delta",       "apply_delta",  "velocity",     "xsph",
     "finalize",      "permute_all",  "gather",      "scatter_ids",  "voxelize",     "bitonic_sort",
+    "row_bounds",
 };
 
 // Slices of the constant copy of the segment table, per device: a batch
@@ -189,6 +190,8 @@ int Ctx::allocate()
   FLOWX_ALLOC(d_src_slot, n)
   FLOWX_ALLOC(d.row_masks, n * 9) FLOWX_ALLOC(d.row_wide, n) FLOWX_ALLOC(d.cell_lo, c) FLOWX_ALLOC(d.cell_hi, c)
   FLOWX_ALLOC(d.quads, (n + 3) / 4) FLOWX_ALLOC(d.plam, n) FLOWX_ALLOC(d.xv, n) FLOWX_ALLOC(d.slot_seg, n)
+  FLOWX_ALLOC(d.quad_bounds, (n + 3) / 4) FLOWX_ALLOC(d.row_yz, c) FLOWX_ALLOC(d.sort_x, n)
+  FLOWX_ALLOC(d.quads_alt, (n + 3) / 4)
   if (flags & FLOWX_FLAG_REFERENCE_ORDER) {
     // solver/sph.py's sorted_count: the next power of two >= N, at least 2
     size_t S = 2;
@@ -206,6 +209,8 @@ int Ctx::allocate()
   d.warp_passes = (flags & FLOWX_FLAG_WARP_PASSES) ? 1
                   : (flags & FLOWX_FLAG_THREAD_PASSES) ? 0
                   : (total_particles <= FLOWX_WARP_PASSES_MAX_PARTICLES ? 1 : 0);
+  d.trim = 0;  // set with the segment table (upload_segs)
+  d.x_order = 0;
   // ids start as the identity: slot k holds particle k.
   std::vector<uint32_t> ident(n);
   for (size_t k = 0; k < n; ++k) ident[k] = (uint32_t)k;
@@ -226,7 +231,7 @@ void Ctx::release()
                   d.delta,  d.delta_alt, d.lam,     d.lam_alt,  d.stage,    d.keys,    d.ids,        d.key_tmp,
                   d.rank_tmp, d.pairs, d.pairs_tmp, d.counts,   d.offsets,  d.block_sums, d.big_cells, d.collider,
                   d.surface, d_segs,   d_src_slot,  d_prims,  d_mesh,  d.row_masks, d.row_wide, d.cell_lo, d.cell_hi, d.quads, d.plam, d.xv, d.slot_seg,
-                  d.bitonic, d.bitonic_inv};
+                  d.bitonic, d.bitonic_inv, d.quad_bounds, d.row_yz, d.sort_x, d.quads_alt};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (stream) cudaStreamDestroy(stream);
@@ -273,8 +278,15 @@ int Ctx::set_push(const flowx_push *push)
   return upload_segs({s}, (int)cells);
 }
 
-int Ctx::upload_segs(const std::vector<SegParams> &s, int cells)
+int Ctx::upload_segs(const std::vector<SegParams> &s_in, int cells)
 {
+  // number the x-rows (cells of one (y, z)) of the segments consecutively
+  std::vector<SegParams> s = s_in;
+  int xrows = 0;
+  for (auto &q : s) {
+    q.r_begin = xrows;
+    xrows += q.ny * q.nz;
+  }
   const bool same = s.size() == segs.size() && std::memcmp(s.data(), segs.data(), s.size() * sizeof(SegParams)) == 0;
   if (!same || cells != d.cells) next_normals_valid = false;  // reach or geometry changed
   if (!same || !segs_uploaded) {
@@ -312,6 +324,16 @@ int Ctx::upload_segs(const std::vector<SegParams> &s, int cells)
     d.segs = d_segs;
     d.nseg = (int)segs.size();
     d.seg0 = segs.empty() ? SegParams{} : segs[0];
+    // Cells coarser than the reach (1.5 h or more): the thread-per-particle
+    // lambda and XSPH passes trim each stencil row to the particle's reach
+    // and keep windowed masks; the re-associated arithmetic also orders each
+    // cell by x, which makes the windows short (the reference's expressions
+    // keep the (cell, id) order the oracle runs; the reference's network
+    // keeps its own). Cells of h keep the untrimmed walk.
+    bool coarse = false;
+    for (const auto &q : segs) coarse = coarse || q.cell >= 1.5f * q.h;
+    d.trim = (coarse && !d.warp_passes) ? 1 : 0;
+    d.x_order = (d.trim && !(flags & (FLOWX_FLAG_EXACT | FLOWX_FLAG_REFERENCE_ORDER))) ? 1 : 0;
     if (segs.size() > 1) {
       const int need = (int)segs.size();
       if (need > cseg_count) {
@@ -327,6 +349,7 @@ int Ctx::upload_segs(const std::vector<SegParams> &s, int cells)
       }
     }
     drop_graphs();  // their launches carry seg0
+    d.xrows = xrows;
   }
   if (cells != d.cells) {
     if (have_grid && cells != d.cells) have_grid = false;
@@ -338,12 +361,12 @@ int Ctx::upload_segs(const std::vector<SegParams> &s, int cells)
 // ------------------------------------------------------------ grid build
 // Cell order from the keys and the scan: the counting sort's (cell, id)
 // order, or the reference's own network (FLOWX_FLAG_REFERENCE_ORDER).
-void Ctx::issue_cell_order()
+void Ctx::issue_cell_order(bool x_order)
 {
   if (flags & FLOWX_FLAG_REFERENCE_ORDER) {
     g_launches += launch_reference_order(d, stream);
   } else {
-    launch_scatter(d, stream);
+    launch_scatter(d, stream, x_order);
     launch_cell_sort(d, stream);
     g_launches += 3;
   }
@@ -354,7 +377,7 @@ void Ctx::issue_build_from_pred(const float4 *pred)
   launch_key_only(d, pred, stream);
   launch_scan(d, stream);
   g_launches += 4;
-  issue_cell_order();
+  issue_cell_order(false);
 }
 
 int Ctx::build_grid_generic()
@@ -400,18 +423,27 @@ int Ctx::issue_substep(int iterations, int pred_in_idx, bool normals_ready)
   }
   launch_predict_key(d, d.normal_alt, stream);
   launch_scan(d, stream);
-  issue_cell_order();
+  issue_cell_order(d.x_order != 0);
   launch_permute_step(d, d.pred_a, d.normal_alt, stream);
   g_launches += 5;
   float4 *q_in = d.pred_a, *q_out = d.pred_b;
   for (int it = 0; it < iterations; ++it) {
+    if (d.trim) {
+      launch_row_bounds(d, q_in, stream);
+      g_launches += 1;
+    }
     launch_lambda_f(d, q_in, exact, stream);
     launch_delta_apply_f(d, q_in, q_out, exact, it == iterations - 1, stream);
     g_launches += 2;
     std::swap(q_in, q_out);
+    if (d.trim) std::swap(d.quads, d.quads_alt);  // the quads of q_in, written by that delta_apply
   }
   if (iterations == 0) {
     launch_xsph_inputs(d, q_in, exact, stream);
+    g_launches += 1;
+  }
+  if (d.trim) {
+    launch_row_bounds(d, q_in, stream);
     g_launches += 1;
   }
   launch_xsph_finalize_f(d, q_in, d.pos, (flags & FLOWX_FLAG_KEEP_DELTA) != 0, exact, sigma, stream);
@@ -642,7 +674,10 @@ int flowx_run_pass(flowx_ctx *ctx, int pass_id, const flowx_push *push)
       c->normal_zero = false;
       break;
     case FLOWX_PASS_PREDICT: launch_predict(d, pred, c->stream); break;
-    case FLOWX_PASS_LAMBDA: launch_lambda(d, pred, c->stream); break;
+    case FLOWX_PASS_LAMBDA:
+      launch_lambda(d, pred, c->stream);  // with the quads' fill and, trimming, the row bounds
+      g_launches += 1 + (d.trim ? 1 : 0);
+      break;
     case FLOWX_PASS_DELTA:
       launch_delta(d, pred, c->stream);
       c->delta_in_order = true;

@@ -71,7 +71,8 @@ struct Ctx {
   float4 *pred_cur();
   int set_push(const flowx_push *push);
   int upload_segs(const std::vector<SegParams> &s, int cells);
-  void issue_cell_order();
+  // scatter + cell sort (x_order: cells by predicted x), or the reference's network
+  void issue_cell_order(bool x_order);
   void issue_build_from_pred(const float4 *pred);
   int build_grid_generic();
   int issue_substep(int iterations, int pred_in_idx, bool normals_ready);

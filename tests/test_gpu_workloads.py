@@ -154,6 +154,27 @@ def test_large_after_sixty_frames(large):
     _check(large, state, large.collider_grid(60), "large after 60 frames")
 
 
+@pytest.fixture(scope="module")
+def coarse():
+    """The large scene's domain and particle spacing with the reference's own
+    cell rule (cells of 0.045 m = 2.25 h, 45^3), a 60 x 60 x 30 block of it:
+    ~91 particles per cell, stencil rows of ~270 slots, the walk that trims
+    each row to the particle's reach."""
+    sc = scenes.large(cell_rule="reference", counts=(60, 60, 30))
+    assert sc.config.cell_size >= 2.0 * sc.config.smoothing_radius
+    return sc
+
+
+def test_coarse_cells_seeded(coarse):
+    _check_reference_order(coarse, _seeded(coarse), coarse.collider_grid(0), "coarse cells seeded")
+    _check(coarse, _seeded(coarse), coarse.collider_grid(0), "coarse cells seeded")
+
+
+def test_coarse_cells_after_twelve_frames(coarse):
+    state = _after_frames(coarse, 12)
+    _check(coarse, state, coarse.collider_grid(12), "coarse cells after 12 frames")
+
+
 def test_pool_seeded(pool):
     _check_reference_order(pool, _seeded(pool), pool.collider_grid(0), "pool seeded")
     _check(pool, _seeded(pool), pool.collider_grid(0), "pool seeded")
