@@ -45,6 +45,12 @@ constexpr int kSmallCellSort = 64;      // cells above this go to the block sort
 // one cell). The key column, cell ranges and membership stay exact; the
 // reference's unstable bitonic sort leaves such a cell in arbitrary order too.
 constexpr int kMaxRankSortCell = 4096;
+// The trimmed walk (cells coarser than the reach) records at most this many
+// chunks per slot for the pass that replays them; a slot with more (or a row
+// over MAX_CELL_SCAN, walked directly) is marked kChunksNotRecorded and the
+// replaying pass walks it again.
+constexpr int kMaxChunks = 16;
+constexpr uint8_t kChunksNotRecorded = 0xff;
 
 // Per-segment parameters, resolved on the host from the push-constant block
 // (shaders/sph_common.glsl:10-17). Kernel constants that depend only on the
@@ -158,7 +164,10 @@ struct DeviceState {
   float *surface;
   float4 *cell_lo, *cell_hi;  // per cell: bounds of its particles' positions (the splat's cell test)
   unsigned long long *row_masks;  // the lambda pass's neighbour masks, 9 per slot (row-major)
-  uint8_t *row_wide;        // per slot: masks not recorded (a row over 64 slots)
+  uint8_t *row_wide;        // per slot: masks not recorded (a row over 64 slots); trimmed walk: the
+                            // number of chunks recorded, or kChunksNotRecorded
+  unsigned long long *chunk_masks;  // trimmed walk (trim): the lambda pass's non-empty chunk masks,
+  uint32_t *chunk_base;             // kMaxChunks per slot (chunk-major), and each one's first slot
   float4 *plam;             // per slot: predicted position and lambda of the last lambda pass
   float4 *xv;               // per slot: velocity (pred - pos) / dt and max(rho, 1e-6) entering XSPH
   SlotQuad *quads;          // ceil(n / 4) groups: the predicted positions the next lambda or

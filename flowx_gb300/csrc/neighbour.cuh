@@ -232,6 +232,19 @@ __device__ __forceinline__ bool build_row_masks_quads(const SegParams &s, const 
   return true;
 }
 
+// Row masks one pass leaves for a later pass that tests the same positions
+// against the same grid with the same reach (the lambda and delta passes of
+// one Jacobi iteration): nine masks per slot, masks[r * n + slot], and a flag
+// for particles that took the per-row walk.
+struct MaskRecord {
+  unsigned long long *masks;
+  uint8_t *wide;
+  int n;
+  unsigned long long *chunk_masks;  // the trimmed walk's: its non-empty chunks, chunk_masks[j * n + slot]
+  uint32_t *chunk_base;             // and the first slot of each
+};
+
+
 // The walk for cells coarser than the reach (rows of more than 64 slots):
 // each stencil row's run trimmed to the particle's reach, then tested and
 // visited sixteen quads at a time (a 64-bit mask in registers per chunk,
@@ -252,11 +265,16 @@ __device__ __forceinline__ bool build_row_masks_quads(const SegParams &s, const 
 // x-ordered cells of the re-associated build make the trimmed runs short. A
 // row above the reference's MAX_CELL_SCAN is walked cell by cell with the
 // cap, as for_each_within_rows does.
-template <bool EXACT, class F>
+//
+// REC: also records the non-empty chunks (mask and first slot) of slot i in
+// rec, so that a later pass over the same positions can replay them.
+template <bool EXACT, bool REC = false, class F>
 __device__ __forceinline__ void for_each_within_trimmed(const SegParams &s, const uint32_t *__restrict__ off,
                                                         const SlotQuad *__restrict__ quads, RowTrim trim, float4 p,
-                                                        float lim2, int3 base, F &&f)
+                                                        float lim2, int3 base, F &&f, MaskRecord rec = {}, int i = 0)
 {
+  uint32_t recorded = 0;
+  bool unrecorded = false;
   const int x0 = max(base.x - 1, 0), x1 = min(base.x + 1, s.nx - 1);
   const float2 npx = make_float2(-p.x, -p.x), npy = make_float2(-p.y, -p.y), npz = make_float2(-p.z, -p.z);
   const float reach2 = lim2 * (1.0f + 0x1p-10f);
@@ -270,6 +288,7 @@ __device__ __forceinline__ void for_each_within_trimmed(const SegParams &s, cons
     const uint32_t rb = __ldg(&off[row + x1 + 1]);
     if (rb <= ra) continue;
     if (rb - ra > (uint32_t)kMaxCellScan) {
+      unrecorded = true;
 #pragma unroll 1
       for (int x = x0; x <= x1; ++x) {
         const uint32_t cs = __ldg(&off[row + x]);
@@ -315,6 +334,15 @@ __device__ __forceinline__ void for_each_within_trimmed(const SegParams &s, cons
       const uint32_t wb = 4u * c0;
       if (ra > wb) m &= ~((1ull << (ra - wb)) - 1ull);       // slots before the row
       if (rb - wb < 4u * nq) m &= (1ull << (rb - wb)) - 1ull;  // slots past it
+      if (REC && m != 0ull) {
+        if (recorded < (uint32_t)kMaxChunks) {
+          rec.chunk_masks[(size_t)recorded * rec.n + i] = m;
+          rec.chunk_base[(size_t)recorded * rec.n + i] = wb;
+          ++recorded;
+        } else {
+          unrecorded = true;
+        }
+      }
 #pragma unroll 1
       while (m) {
         const int t = __ffsll((long long)m) - 1;
@@ -322,6 +350,37 @@ __device__ __forceinline__ void for_each_within_trimmed(const SegParams &s, cons
         f((int)(wb + (uint32_t)t), true);
       }
     }
+  }
+  if (REC) rec.wide[i] = unrecorded ? kChunksNotRecorded : (uint8_t)recorded;
+}
+
+// Phase 2 from slot i's recorded chunks (for_each_within_trimmed with REC,
+// left by the launch just before on the same stream: same positions, grid
+// and reach), flattened across chunks; a slot marked kChunksNotRecorded walks
+// its trimmed rows again.
+template <bool EXACT, class F>
+__device__ __forceinline__ void visit_recorded_chunks(const SegParams &s, const uint32_t *__restrict__ off,
+                                                      const SlotQuad *__restrict__ quads, RowTrim trim, float4 p,
+                                                      float lim2, int3 base, MaskRecord rec, int i, F &&f)
+{
+  const uint8_t count = __ldg(&rec.wide[i]);
+  if (count == kChunksNotRecorded) {
+    for_each_within_trimmed<EXACT>(s, off, quads, trim, p, lim2, base, f);
+    return;
+  }
+  uint32_t j = 0, wb = 0;
+  unsigned long long m = 0ull;
+#pragma unroll 1
+  while (true) {
+    if (m == 0ull) {
+      if (j >= count) break;
+      m = __ldg(&rec.chunk_masks[(size_t)j * rec.n + i]);
+      wb = __ldg(&rec.chunk_base[(size_t)j * rec.n + i]);
+      ++j;
+    }
+    const int t = __ffsll((long long)m) - 1;
+    m &= m - 1ull;
+    f((int)(wb + (uint32_t)t), true);
   }
 }
 
@@ -369,16 +428,6 @@ __device__ __forceinline__ void for_each_within(const SegParams &s, const uint32
     for_each_within_rows<EXACT>(s, off, pos, p, lim2, base, f);
 }
 
-// Row masks one pass leaves for a later pass that tests the same positions
-// against the same grid with the same reach (the lambda and delta passes of
-// one Jacobi iteration): nine masks per slot, masks[r * n + slot], and a flag
-// for particles that took the per-row walk.
-struct MaskRecord {
-  unsigned long long *masks;
-  uint8_t *wide;
-  int n;
-};
-
 // for_each_within with phase 1 over the slot quads (quads[k / 4] lane k % 4
 // holding pos[k]).
 // WIN: cells coarser than the reach, the trimmed walk (for_each_within_trimmed).
@@ -407,8 +456,8 @@ __device__ __forceinline__ void for_each_within_recording(const SegParams &s, co
                                                           const SlotQuad *__restrict__ quads, RowTrim trim, float4 p,
                                                           float lim2, int3 base, MaskRecord rec, int i, F &&f)
 {
-  if (WIN) {  // nothing recorded: the delta pass walks its trimmed rows too
-    for_each_within_trimmed<EXACT>(s, off, quads, trim, p, lim2, base, f);
+  if (WIN) {
+    for_each_within_trimmed<EXACT, true>(s, off, quads, trim, p, lim2, base, f, rec, i);
     return;
   }
   extern __shared__ unsigned long long row_masks[];
@@ -427,7 +476,7 @@ __device__ __forceinline__ void for_each_within_recording(const SegParams &s, co
 
 // for_each_within from slot i's recorded masks, left by the launch just
 // before on the same stream (same positions, grid and reach): phase 2 only.
-// WIN (nothing recorded): the trimmed walk over the same positions' quads.
+// WIN: the recording launch's chunks (visit_recorded_chunks).
 template <bool EXACT, bool WIN, class F>
 __device__ __forceinline__ void for_each_within_recorded(const SegParams &s, const uint32_t *__restrict__ off,
                                                          const float4 *__restrict__ pos,
@@ -435,7 +484,7 @@ __device__ __forceinline__ void for_each_within_recorded(const SegParams &s, con
                                                          float lim2, int3 base, MaskRecord rec, int i, F &&f)
 {
   if (WIN) {
-    for_each_within_trimmed<EXACT>(s, off, quads, trim, p, lim2, base, f);
+    visit_recorded_chunks<EXACT>(s, off, quads, trim, p, lim2, base, rec, i, f);
     return;
   }
   extern __shared__ unsigned long long row_masks[];

@@ -49,7 +49,7 @@ __global__ void __launch_bounds__(512, 3) k_lambda_f(DeviceState d, const float4
   const float4 pi = pred[i];
   const int3 base = cell_coord(s, pi.x, pi.y, pi.z);
   LambdaAcc<EXACT> acc;
-  const MaskRecord rec{d.row_masks, d.row_wide, d.n};
+  const MaskRecord rec{d.row_masks, d.row_wide, d.n, d.chunk_masks, d.chunk_base};
   const RowTrim trim{d.quad_bounds, d.row_yz};
   for_each_within_recording<EXACT, WIN>(s, d.offsets, pred, d.quads, trim, pi, s.h2, base, rec, i, [&](int k, bool within) {
     const float4 pj = __ldg(&pred[k]);
@@ -85,7 +85,7 @@ __device__ __forceinline__ float3 delta_sum_f(const SegParams &s, const DeviceSt
   };
   if (RECORDED)
     for_each_within_recorded<EXACT, WIN>(s, d.offsets, pred, d.quads, RowTrim{d.quad_bounds, d.row_yz}, pi, h2,
-                                         base, MaskRecord{d.row_masks, d.row_wide, d.n}, i, body);
+                                         base, MaskRecord{d.row_masks, d.row_wide, d.n, d.chunk_masks, d.chunk_base}, i, body);
   else
     for_each_within<EXACT>(s, d.offsets, pred, pi, h2, base, body);
   return make_float3(ax, ay, az);

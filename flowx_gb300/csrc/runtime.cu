@@ -231,7 +231,8 @@ void Ctx::release()
                   d.delta,  d.delta_alt, d.lam,     d.lam_alt,  d.stage,    d.keys,    d.ids,        d.key_tmp,
                   d.rank_tmp, d.pairs, d.pairs_tmp, d.counts,   d.offsets,  d.block_sums, d.big_cells, d.collider,
                   d.surface, d_segs,   d_src_slot,  d_prims,  d_mesh,  d.row_masks, d.row_wide, d.cell_lo, d.cell_hi, d.quads, d.plam, d.xv, d.slot_seg,
-                  d.bitonic, d.bitonic_inv, d.quad_bounds, d.row_yz, d.sort_x, d.quads_alt};
+                  d.bitonic, d.bitonic_inv, d.quad_bounds, d.row_yz, d.sort_x, d.quads_alt,
+                  d.chunk_masks, d.chunk_base};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (stream) cudaStreamDestroy(stream);
@@ -333,6 +334,12 @@ int Ctx::upload_segs(const std::vector<SegParams> &s_in, int cells)
     bool coarse = false;
     for (const auto &q : segs) coarse = coarse || q.cell >= 1.5f * q.h;
     d.trim = (coarse && !d.warp_passes) ? 1 : 0;
+    if (d.trim && !d.chunk_masks) {  // the trimmed walk's chunk record, on first use
+      const size_t n = (size_t)std::max(total_particles, 1) * kMaxChunks;
+      cudaError_t e = dalloc(&d.chunk_masks, n);
+      if (e == cudaSuccess) e = dalloc(&d.chunk_base, n);
+      if (e != cudaSuccess) return cuda(e, "chunk record allocation");
+    }
     d.x_order = (d.trim && !(flags & (FLOWX_FLAG_EXACT | FLOWX_FLAG_REFERENCE_ORDER))) ? 1 : 0;
     if (segs.size() > 1) {
       const int need = (int)segs.size();
