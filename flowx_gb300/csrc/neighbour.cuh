@@ -430,13 +430,13 @@ __device__ __forceinline__ void for_each_within(const SegParams &s, const uint32
 
 // for_each_within with phase 1 over the slot quads (quads[k / 4] lane k % 4
 // holding pos[k]).
-// WIN: cells coarser than the reach, the trimmed walk (for_each_within_trimmed).
-template <bool EXACT, bool WIN, class F>
+// TRIMMED: cells coarser than the reach, the trimmed walk (for_each_within_trimmed).
+template <bool EXACT, bool TRIMMED, class F>
 __device__ __forceinline__ void for_each_within(const SegParams &s, const uint32_t *__restrict__ off,
                                                 const float4 *__restrict__ pos, const SlotQuad *__restrict__ quads,
                                                 RowTrim trim, float4 p, float lim2, int3 base, F &&f)
 {
-  if (WIN) {
+  if (TRIMMED) {
     for_each_within_trimmed<EXACT>(s, off, quads, trim, p, lim2, base, f);
     return;
   }
@@ -450,13 +450,13 @@ __device__ __forceinline__ void for_each_within(const SegParams &s, const uint32
 
 // for_each_within (phase 1 over the slot quads) that also records slot i's
 // masks.
-template <bool EXACT, bool WIN, class F>
+template <bool EXACT, bool TRIMMED, class F>
 __device__ __forceinline__ void for_each_within_recording(const SegParams &s, const uint32_t *__restrict__ off,
                                                           const float4 *__restrict__ pos,
                                                           const SlotQuad *__restrict__ quads, RowTrim trim, float4 p,
                                                           float lim2, int3 base, MaskRecord rec, int i, F &&f)
 {
-  if (WIN) {
+  if (TRIMMED) {
     for_each_within_trimmed<EXACT, true>(s, off, quads, trim, p, lim2, base, f, rec, i);
     return;
   }
@@ -476,14 +476,14 @@ __device__ __forceinline__ void for_each_within_recording(const SegParams &s, co
 
 // for_each_within from slot i's recorded masks, left by the launch just
 // before on the same stream (same positions, grid and reach): phase 2 only.
-// WIN: the recording launch's chunks (visit_recorded_chunks).
-template <bool EXACT, bool WIN, class F>
+// TRIMMED: the recording launch's chunks (visit_recorded_chunks).
+template <bool EXACT, bool TRIMMED, class F>
 __device__ __forceinline__ void for_each_within_recorded(const SegParams &s, const uint32_t *__restrict__ off,
                                                          const float4 *__restrict__ pos,
                                                          const SlotQuad *__restrict__ quads, RowTrim trim, float4 p,
                                                          float lim2, int3 base, MaskRecord rec, int i, F &&f)
 {
-  if (WIN) {
+  if (TRIMMED) {
     visit_recorded_chunks<EXACT>(s, off, quads, trim, p, lim2, base, rec, i, f);
     return;
   }

@@ -42,7 +42,7 @@ static inline unsigned grid_for(long long n, int b) { return (unsigned)((n + b -
 // latency than the few registers cost, 1.6% per frame), delta_apply four
 // (32), XSPH five 256-thread blocks (48).
 // sph_lambda.glsl:17-77
-template <bool EXACT, int SEG, bool WIN>
+template <bool EXACT, int SEG, bool TRIMMED>
 __global__ void __launch_bounds__(512, 3) k_lambda_f(DeviceState d, const float4 *__restrict__ pred)
 {
   FLOWX_SLOT_PROLOGUE_SEG
@@ -51,7 +51,7 @@ __global__ void __launch_bounds__(512, 3) k_lambda_f(DeviceState d, const float4
   LambdaAcc<EXACT> acc;
   const MaskRecord rec{d.row_masks, d.row_wide, d.n, d.chunk_masks, d.chunk_base};
   const RowTrim trim{d.quad_bounds, d.row_yz};
-  for_each_within_recording<EXACT, WIN>(s, d.offsets, pred, d.quads, trim, pi, s.h2, base, rec, i, [&](int k, bool within) {
+  for_each_within_recording<EXACT, TRIMMED>(s, d.offsets, pred, d.quads, trim, pi, s.h2, base, rec, i, [&](int k, bool within) {
     const float4 pj = __ldg(&pred[k]);
     acc.pair(s, pi.x - pj.x, pi.y - pj.y, pi.z - pj.z, within);
   });
@@ -66,7 +66,7 @@ __global__ void __launch_bounds__(512, 3) k_lambda_f(DeviceState d, const float4
 // in for phase 1; the body keeps its own j != i and r^2 > 1e-12 tests.
 // RECORDED also reads each neighbour's position and lambda from d.plam (one
 // 16-byte load; the lambda pass left them there).
-template <bool EXACT, bool RECORDED, bool WIN = false>
+template <bool EXACT, bool RECORDED, bool TRIMMED = false>
 __device__ __forceinline__ float3 delta_sum_f(const SegParams &s, const DeviceState &d, const float4 *__restrict__ pred,
                                               int i, float4 pi)
 {
@@ -84,7 +84,7 @@ __device__ __forceinline__ float3 delta_sum_f(const SegParams &s, const DeviceSt
     delta_pair<EXACT>(s, lambda_i, RECORDED ? pj.w : __ldg(&d.lam[k].y), dx, dy, dz, r2, ax, ay, az);
   };
   if (RECORDED)
-    for_each_within_recorded<EXACT, WIN>(s, d.offsets, pred, d.quads, RowTrim{d.quad_bounds, d.row_yz}, pi, h2,
+    for_each_within_recorded<EXACT, TRIMMED>(s, d.offsets, pred, d.quads, RowTrim{d.quad_bounds, d.row_yz}, pi, h2,
                                          base, MaskRecord{d.row_masks, d.row_wide, d.n, d.chunk_masks, d.chunk_base}, i, body);
   else
     for_each_within<EXACT>(s, d.offsets, pred, pi, h2, base, body);
@@ -126,17 +126,17 @@ __device__ __forceinline__ void normal_terms(const SegParams &s, float rho_j, fl
 // gathers are latency-bound, and the full 64 resident warps hide more of them
 // (0.726 -> 0.688 ms per launch on the 4M-particle workload); the reference
 // form would spill at 32 and keeps three.
-template <bool EXACT, int SEG, bool WIN>
+template <bool EXACT, int SEG, bool TRIMMED>
 __global__ void __launch_bounds__(512, EXACT ? 3 : 4) k_delta_apply_f(DeviceState d, const float4 *__restrict__ pred_in,
                                                        float4 *__restrict__ pred_out, int last)
 {
   FLOWX_SLOT_PROLOGUE_SEG
   const float4 pi = pred_in[i];
-  const float3 a = delta_sum_f<EXACT, true, WIN>(s, d, pred_in, i, pi);
+  const float3 a = delta_sum_f<EXACT, true, TRIMMED>(s, d, pred_in, i, pi);
   const float rest = s.rest;
   const float4 q = make_float4(pi.x + a.x / rest, pi.y + a.y / rest, pi.z + a.z / rest, 1.0f);
   pred_out[i] = q;
-  store_quad(WIN ? d.quads_alt : d.quads, i, q.x, q.y, q.z);
+  store_quad(TRIMMED ? d.quads_alt : d.quads, i, q.x, q.y, q.z);
   if (last) d.xv[i] = xsph_input<EXACT>(s, d, i, q);
 }
 
@@ -260,7 +260,7 @@ void launch_row_bounds(const DeviceState &d, const float4 *pred, cudaStream_t st
 // them - and leaves the result in *normal_out.
 // The fused pass (QUADS) takes each neighbour's velocity and density from
 // d.xv, left by the last delta_apply.
-template <bool EXACT, bool QUADS, bool NORMALS, bool WIN = false, class VelJ>
+template <bool EXACT, bool QUADS, bool NORMALS, bool TRIMMED = false, class VelJ>
 __device__ __forceinline__ float3 xsph_sum_f(const SegParams &s, const DeviceState &d, const float4 *__restrict__ pred,
                                              int i, float4 q, float3 vi, VelJ &&velj, float4 *normal_out = nullptr)
 {
@@ -301,7 +301,7 @@ __device__ __forceinline__ float3 xsph_sum_f(const SegParams &s, const DeviceSta
     if (normals) normal_terms<EXACT>(s, rho_j, r2, dx, dy, dz, nx, ny, nz, lap);  // sph_normal.glsl's body
   };
   if (QUADS)
-    for_each_within<EXACT, WIN>(s, d.offsets, pred, d.quads, RowTrim{d.quad_bounds, d.row_yz}, q, h2, base, body);
+    for_each_within<EXACT, TRIMMED>(s, d.offsets, pred, d.quads, RowTrim{d.quad_bounds, d.row_yz}, q, h2, base, body);
   else
     for_each_within<EXACT>(s, d.offsets, pred, q, h2, base, body);
   if (normals) {
@@ -318,7 +318,7 @@ __device__ __forceinline__ float3 xsph_sum_f(const SegParams &s, const DeviceSta
 // of this grid, which the next substep's permute maps to its own). Bounded to
 // five 256-thread blocks per SM (48 registers): with both bodies it spills at
 // 40 (1.68 -> 1.63 ms per launch on the 4M-particle workload).
-template <bool EXACT, bool NORMALS, int SEG, bool WIN>
+template <bool EXACT, bool NORMALS, int SEG, bool TRIMMED>
 __global__ void __launch_bounds__(256, 5) k_xsph_finalize_f(DeviceState d, const float4 *__restrict__ pred,
                                                          float4 *__restrict__ pos_out, int keep_delta)
 {
@@ -326,7 +326,7 @@ __global__ void __launch_bounds__(256, 5) k_xsph_finalize_f(DeviceState d, const
   const float4 q = pred[i];
   const float4 xi = d.xv[i];
   const float3 vi = make_float3(xi.x, xi.y, xi.z);
-  const float3 dv = xsph_sum_f<EXACT, true, NORMALS, WIN>(
+  const float3 dv = xsph_sum_f<EXACT, true, NORMALS, TRIMMED>(
       s, d, pred, i, q, vi, [](int, const float4 &) { return make_float3(0.f, 0.f, 0.f); }, d.normal_alt + i);
   float3 v = make_float3(vi.x + dv.x, vi.y + dv.y, vi.z + dv.z);
   float3 p = make_float3(q.x, q.y, q.z);
@@ -362,11 +362,10 @@ __global__ void __launch_bounds__(512, 3) k_normal_f(DeviceState d, const float4
   out[i] = make_float4(nx, ny, nz, curv);
 }
 
-// f(std::bool_constant<WIN>): windowed masks over trimmed rows when the
-// context's cells are coarser than the reach (d.trim), the plain row masks
-// otherwise.
+// f(std::bool_constant<TRIMMED>): the trimmed walk when the context's cells
+// are coarser than the reach (d.trim), the plain row masks otherwise.
 template <class F>
-static void with_windows(const DeviceState &d, F &&f)
+static void with_trimmed_walk(const DeviceState &d, F &&f)
 {
   if (d.trim)
     f(std::true_type{});
@@ -379,14 +378,14 @@ void launch_lambda_f(const DeviceState &d, const float4 *pred, bool exact, cudaS
   if (d.warp_passes) return launch_lambda_w(d, pred, exact, st);
   if (d.n <= 0) return;
   with_seg_source(d, [&](auto tag) {
-    with_windows(d, [&](auto wtag) {
+    with_trimmed_walk(d, [&](auto wtag) {
       constexpr int SEG = decltype(tag)::value;
-      constexpr bool WIN = decltype(wtag)::value;
-      const void *fn = exact ? (const void *)k_lambda_f<true, SEG, WIN> : (const void *)k_lambda_f<false, SEG, WIN>;
+      constexpr bool TRIMMED = decltype(wtag)::value;
+      const void *fn = exact ? (const void *)k_lambda_f<true, SEG, TRIMMED> : (const void *)k_lambda_f<false, SEG, TRIMMED>;
       const int b = FLOWX_BLOCK(d, K_LAMBDA, 128, fn);
       const unsigned g = grid_for(d.n, b);
-      if (exact) k_lambda_f<true, SEG, WIN><<<g, b, row_mask_bytes(b), st>>>(d, pred);
-      else k_lambda_f<false, SEG, WIN><<<g, b, row_mask_bytes(b), st>>>(d, pred);
+      if (exact) k_lambda_f<true, SEG, TRIMMED><<<g, b, row_mask_bytes(b), st>>>(d, pred);
+      else k_lambda_f<false, SEG, TRIMMED><<<g, b, row_mask_bytes(b), st>>>(d, pred);
     });
   });
 }
@@ -397,15 +396,15 @@ void launch_delta_apply_f(const DeviceState &d, const float4 *pred_in, float4 *p
   if (d.n <= 0) return;
   const int l = last ? 1 : 0;
   with_seg_source(d, [&](auto tag) {
-    with_windows(d, [&](auto wtag) {
+    with_trimmed_walk(d, [&](auto wtag) {
       constexpr int SEG = decltype(tag)::value;
-      constexpr bool WIN = decltype(wtag)::value;
+      constexpr bool TRIMMED = decltype(wtag)::value;
       const void *fn =
-          exact ? (const void *)k_delta_apply_f<true, SEG, WIN> : (const void *)k_delta_apply_f<false, SEG, WIN>;
+          exact ? (const void *)k_delta_apply_f<true, SEG, TRIMMED> : (const void *)k_delta_apply_f<false, SEG, TRIMMED>;
       const int b = FLOWX_BLOCK(d, K_DELTA_APPLY, 128, fn);
       const unsigned g = grid_for(d.n, b);
-      if (exact) k_delta_apply_f<true, SEG, WIN><<<g, b, row_mask_bytes(b), st>>>(d, pred_in, pred_out, l);
-      else k_delta_apply_f<false, SEG, WIN><<<g, b, row_mask_bytes(b), st>>>(d, pred_in, pred_out, l);
+      if (exact) k_delta_apply_f<true, SEG, TRIMMED><<<g, b, row_mask_bytes(b), st>>>(d, pred_in, pred_out, l);
+      else k_delta_apply_f<false, SEG, TRIMMED><<<g, b, row_mask_bytes(b), st>>>(d, pred_in, pred_out, l);
     });
   });
 }
@@ -420,12 +419,12 @@ static void xsph_finalize_launch(const DeviceState &d, const float4 *pred, float
                                  cudaStream_t st)
 {
   with_seg_source(d, [&](auto tag) {
-    with_windows(d, [&](auto wtag) {
+    with_trimmed_walk(d, [&](auto wtag) {
       constexpr int SEG = decltype(tag)::value;
-      constexpr bool WIN = decltype(wtag)::value;
-      const void *fn = (const void *)k_xsph_finalize_f<EXACT, NORMALS, SEG, WIN>;
+      constexpr bool TRIMMED = decltype(wtag)::value;
+      const void *fn = (const void *)k_xsph_finalize_f<EXACT, NORMALS, SEG, TRIMMED>;
       const int b = FLOWX_BLOCK(d, K_XSPH_FINALIZE, 128, fn);
-      k_xsph_finalize_f<EXACT, NORMALS, SEG, WIN><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred, pos_out,
+      k_xsph_finalize_f<EXACT, NORMALS, SEG, TRIMMED><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred, pos_out,
                                                                                                 keep_delta);
     });
   });

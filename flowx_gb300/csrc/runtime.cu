@@ -326,11 +326,11 @@ int Ctx::upload_segs(const std::vector<SegParams> &s_in, int cells)
     d.nseg = (int)segs.size();
     d.seg0 = segs.empty() ? SegParams{} : segs[0];
     // Cells coarser than the reach (1.5 h or more): the thread-per-particle
-    // lambda and XSPH passes trim each stencil row to the particle's reach
-    // and keep windowed masks; the re-associated arithmetic also orders each
-    // cell by x, which makes the windows short (the reference's expressions
-    // keep the (cell, id) order the oracle runs; the reference's network
-    // keeps its own). Cells of h keep the untrimmed walk.
+    // neighbour passes trim each stencil row to the particle's reach
+    // (for_each_within_trimmed); the re-associated arithmetic also orders
+    // each cell by x, which makes the trimmed runs short (the reference's
+    // expressions keep the (cell, id) order the oracle runs; the reference's
+    // network keeps its own). Cells of h keep the untrimmed walk.
     bool coarse = false;
     for (const auto &q : segs) coarse = coarse || q.cell >= 1.5f * q.h;
     d.trim = (coarse && !d.warp_passes) ? 1 : 0;
