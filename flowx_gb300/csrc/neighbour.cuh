@@ -268,13 +268,23 @@ struct MaskRecord {
 //
 // REC: also records the non-empty chunks (mask and first slot) of slot i in
 // rec, so that a later pass over the same positions can replay them.
-template <bool EXACT, bool REC = false, class F>
+// STAGE: the chunks are kept in shared memory (up to kRows, masks in the row
+// mask slots, first slots after them: trimmed_walk_bytes) and visited after
+// all rows, flattened across chunks; a slot with more chunks, or with a row
+// over MAX_CELL_SCAN, is walked again chunk by chunk.
+template <bool EXACT, bool REC = false, bool STAGE = false, class F>
 __device__ __forceinline__ void for_each_within_trimmed(const SegParams &s, const uint32_t *__restrict__ off,
                                                         const SlotQuad *__restrict__ quads, RowTrim trim, float4 p,
                                                         float lim2, int3 base, F &&f, MaskRecord rec = {}, int i = 0)
 {
   uint32_t recorded = 0;
   bool unrecorded = false;
+  extern __shared__ unsigned long long row_masks[];
+  unsigned long long *sm = row_masks + threadIdx.x;
+  uint32_t *sb = reinterpret_cast<uint32_t *>(row_masks + kRows * blockDim.x) + threadIdx.x;
+  const int stride = blockDim.x;
+  uint32_t staged = 0;
+  bool overflow = false;
   const int x0 = max(base.x - 1, 0), x1 = min(base.x + 1, s.nx - 1);
   const float2 npx = make_float2(-p.x, -p.x), npy = make_float2(-p.y, -p.y), npz = make_float2(-p.z, -p.z);
   const float reach2 = lim2 * (1.0f + 0x1p-10f);
@@ -289,6 +299,10 @@ __device__ __forceinline__ void for_each_within_trimmed(const SegParams &s, cons
     if (rb <= ra) continue;
     if (rb - ra > (uint32_t)kMaxCellScan) {
       unrecorded = true;
+      if (STAGE) {  // visited in order by the second walk
+        overflow = true;
+        continue;
+      }
 #pragma unroll 1
       for (int x = x0; x <= x1; ++x) {
         const uint32_t cs = __ldg(&off[row + x]);
@@ -343,6 +357,18 @@ __device__ __forceinline__ void for_each_within_trimmed(const SegParams &s, cons
           unrecorded = true;
         }
       }
+      if (STAGE) {
+        if (m != 0ull) {
+          if (staged < (uint32_t)kRows) {
+            sm[staged * stride] = m;
+            sb[staged * stride] = wb;
+            ++staged;
+          } else {
+            overflow = true;
+          }
+        }
+        continue;
+      }
 #pragma unroll 1
       while (m) {
         const int t = __ffsll((long long)m) - 1;
@@ -352,6 +378,32 @@ __device__ __forceinline__ void for_each_within_trimmed(const SegParams &s, cons
     }
   }
   if (REC) rec.wide[i] = unrecorded ? kChunksNotRecorded : (uint8_t)recorded;
+  if (STAGE) {
+    if (overflow) {
+      for_each_within_trimmed<EXACT>(s, off, quads, trim, p, lim2, base, f);
+      return;
+    }
+    uint32_t j = 0, wb = 0;
+    unsigned long long m = 0ull;
+#pragma unroll 1
+    while (true) {
+      if (m == 0ull) {
+        if (j >= staged) break;
+        m = sm[j * stride];
+        wb = sb[j * stride];
+        ++j;
+      }
+      const int t = __ffsll((long long)m) - 1;
+      m &= m - 1ull;
+      f((int)(wb + (uint32_t)t), true);
+    }
+  }
+}
+
+// Dynamic shared memory of a launch using the staged trimmed walk.
+inline size_t trimmed_walk_bytes(int block)
+{
+  return (size_t)block * kRows * (sizeof(unsigned long long) + sizeof(uint32_t));
 }
 
 // Phase 2 from slot i's recorded chunks (for_each_within_trimmed with REC,
@@ -437,7 +489,7 @@ __device__ __forceinline__ void for_each_within(const SegParams &s, const uint32
                                                 RowTrim trim, float4 p, float lim2, int3 base, F &&f)
 {
   if (TRIMMED) {
-    for_each_within_trimmed<EXACT>(s, off, quads, trim, p, lim2, base, f);
+    for_each_within_trimmed<EXACT, false, true>(s, off, quads, trim, p, lim2, base, f);
     return;
   }
   extern __shared__ unsigned long long row_masks[];
@@ -457,7 +509,7 @@ __device__ __forceinline__ void for_each_within_recording(const SegParams &s, co
                                                           float lim2, int3 base, MaskRecord rec, int i, F &&f)
 {
   if (TRIMMED) {
-    for_each_within_trimmed<EXACT, true>(s, off, quads, trim, p, lim2, base, f, rec, i);
+    for_each_within_trimmed<EXACT, true, true>(s, off, quads, trim, p, lim2, base, f, rec, i);
     return;
   }
   extern __shared__ unsigned long long row_masks[];

@@ -212,35 +212,55 @@ __global__ void __launch_bounds__(kRowBoundsBlock) k_row_bounds(DeviceState d, c
                                       fminf(zlo, fminf(zlo_l, zlo_r)), fmaxf(zhi, fmaxf(zhi_l, zhi_r)));
   }
   const uint32_t A = __ldg(&off[row]), B = __ldg(&off[row + s.nx]);
+  // running maximum from the first slot, four 32-slot chunks per step (their
+  // loads issued together)
   float carry = -inf;
 #pragma unroll 1
-  for (uint32_t b0 = A; b0 < B; b0 += 32u) {
-    const uint32_t k = b0 + (uint32_t)lane;
-    float v = k < B ? __ldg(&pred[k]).x : -inf;
+  for (uint32_t b0 = A; b0 < B; b0 += 128u) {
+    float v[4];
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const float t = __shfl_up_sync(full, v, o);
-      if (lane >= o) v = fmaxf(v, t);
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t k = b0 + 32u * (uint32_t)u + (uint32_t)lane;
+      v[u] = k < B ? __ldg(&pred[k]).x : -inf;
     }
-    v = fmaxf(v, carry);
-    carry = __shfl_sync(full, v, 31);
-    if (k < B && (k & 3u) == 3u) d.quad_bounds[k >> 2].x = v;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t k = b0 + 32u * (uint32_t)u + (uint32_t)lane;
+      float x = v[u];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const float t = __shfl_up_sync(full, x, o);
+        if (lane >= o) x = fmaxf(x, t);
+      }
+      x = fmaxf(x, carry);
+      carry = __shfl_sync(full, x, 31);
+      if (k < B && (k & 3u) == 3u) d.quad_bounds[k >> 2].x = x;
+    }
   }
+  // running minimum from the last slot
   carry = inf;
 #pragma unroll 1
-  for (uint32_t t0 = 0; t0 < B - A; t0 += 32u) {
-    const uint32_t t = t0 + (uint32_t)lane;  // slots from the x-row's last
-    const bool in = t < B - A;
-    const uint32_t k = B - 1u - t;
-    float v = in ? __ldg(&pred[k]).x : inf;
+  for (uint32_t t0 = 0; t0 < B - A; t0 += 128u) {
+    float v[4];
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const float u = __shfl_up_sync(full, v, o);
-      if (lane >= o) v = fminf(v, u);
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t t = t0 + 32u * (uint32_t)u + (uint32_t)lane;  // slots from the x-row's last
+      v[u] = t < B - A ? __ldg(&pred[B - 1u - t]).x : inf;
     }
-    v = fminf(v, carry);
-    carry = __shfl_sync(full, v, 31);
-    if (in && (k & 3u) == 0u) d.quad_bounds[k >> 2].y = v;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t t = t0 + 32u * (uint32_t)u + (uint32_t)lane;
+      const uint32_t k = B - 1u - t;
+      float x = v[u];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const float w = __shfl_up_sync(full, x, o);
+        if (lane >= o) x = fminf(x, w);
+      }
+      x = fminf(x, carry);
+      carry = __shfl_sync(full, x, 31);
+      if (t < B - A && (k & 3u) == 0u) d.quad_bounds[k >> 2].y = x;
+    }
   }
 }
 
@@ -384,8 +404,9 @@ void launch_lambda_f(const DeviceState &d, const float4 *pred, bool exact, cudaS
       const void *fn = exact ? (const void *)k_lambda_f<true, SEG, TRIMMED> : (const void *)k_lambda_f<false, SEG, TRIMMED>;
       const int b = FLOWX_BLOCK(d, K_LAMBDA, 128, fn);
       const unsigned g = grid_for(d.n, b);
-      if (exact) k_lambda_f<true, SEG, TRIMMED><<<g, b, row_mask_bytes(b), st>>>(d, pred);
-      else k_lambda_f<false, SEG, TRIMMED><<<g, b, row_mask_bytes(b), st>>>(d, pred);
+      const size_t sh = TRIMMED ? trimmed_walk_bytes(b) : row_mask_bytes(b);
+      if (exact) k_lambda_f<true, SEG, TRIMMED><<<g, b, sh, st>>>(d, pred);
+      else k_lambda_f<false, SEG, TRIMMED><<<g, b, sh, st>>>(d, pred);
     });
   });
 }
@@ -424,8 +445,8 @@ static void xsph_finalize_launch(const DeviceState &d, const float4 *pred, float
       constexpr bool TRIMMED = decltype(wtag)::value;
       const void *fn = (const void *)k_xsph_finalize_f<EXACT, NORMALS, SEG, TRIMMED>;
       const int b = FLOWX_BLOCK(d, K_XSPH_FINALIZE, 128, fn);
-      k_xsph_finalize_f<EXACT, NORMALS, SEG, TRIMMED><<<grid_for(d.n, b), b, row_mask_bytes(b), st>>>(d, pred, pos_out,
-                                                                                                keep_delta);
+      const size_t sh = TRIMMED ? trimmed_walk_bytes(b) : row_mask_bytes(b);
+      k_xsph_finalize_f<EXACT, NORMALS, SEG, TRIMMED><<<grid_for(d.n, b), b, sh, st>>>(d, pred, pos_out, keep_delta);
     });
   });
 }
