@@ -81,6 +81,36 @@ def test_batch_beyond_the_constant_segment_table():
         check(run(b3), n1, "second (released slice)")
 
 
+def test_batch_with_coarse_cells_equals_scenes_stepped_alone():
+    """A batch holding a scene whose cells are coarser than its reach (the
+    reference's own cell rule, 2.25 h) runs the trimmed walk for all its
+    scenes (row bounds per x-row, each x-row finding its scene). Each scene's
+    substeps equal the scene stepped alone, bit for bit (the reference's
+    expressions), the dam break alone taking the untrimmed walk."""
+    from flowx_gb300.batch import Batch
+    from flowx_gb300.sph import Solver
+
+    coarse = scenes.large(cell_rule="reference", counts=(40, 40, 20))
+    assert coarse.config.cell_size >= 2.0 * coarse.config.smoothing_radius
+    sc = [scenes.dam_break(), coarse]
+    nsub = 2
+    with Batch(sc, exact=True) as b:
+        b.build_grid()
+        b.step(4, nsub)
+        got = {name: b.read(name) for name in ("positions", "velocities", "lambda")}
+    lo = 0
+    for k, s in enumerate(sc):
+        col = s.collider_grid(0)
+        with Solver(s.config, s.positions, s.velocities, collider=col,
+                    collider_voxel=s.collider_voxel if col is not None else 0.0, exact=True) as one:
+            one._build_grid(0.0)
+            for _ in range(nsub):
+                one._substep(s.dt)
+            for name, arr in got.items():
+                np.testing.assert_array_equal(arr[lo:lo + s.n], one.read(name), err_msg=f"scene {k} {name}")
+        lo += s.n
+
+
 def test_batch_scene_matches_oracle():
     from flowx_gb300.batch import Batch
 
