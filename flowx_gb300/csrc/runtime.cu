@@ -327,10 +327,12 @@ int Ctx::upload_segs(const std::vector<SegParams> &s_in, int cells)
     d.seg0 = segs.empty() ? SegParams{} : segs[0];
     // Cells coarser than the reach (1.5 h or more): the thread-per-particle
     // neighbour passes trim each stencil row to the particle's reach
-    // (for_each_within_trimmed); the re-associated arithmetic also orders
-    // each cell by x, which makes the trimmed runs short (the reference's
-    // expressions keep the (cell, id) order the oracle runs; the reference's
-    // network keeps its own). Cells of h keep the untrimmed walk.
+    // (for_each_within_trimmed); cells of h keep the untrimmed walk. The
+    // re-associated arithmetic orders each cell by x, which makes the trimmed
+    // runs short and, on cells of h, gives a warp's lanes more alike
+    // neighbourhoods (0.6% per frame on the 4M workload); the reference's
+    // expressions keep the (cell, id) order the oracle runs, and the
+    // reference's network keeps its own.
     bool coarse = false;
     for (const auto &q : segs) coarse = coarse || q.cell >= 1.5f * q.h;
     d.trim = (coarse && !d.warp_passes) ? 1 : 0;
@@ -340,7 +342,7 @@ int Ctx::upload_segs(const std::vector<SegParams> &s_in, int cells)
       if (e == cudaSuccess) e = dalloc(&d.chunk_base, n);
       if (e != cudaSuccess) return cuda(e, "chunk record allocation");
     }
-    d.x_order = (d.trim && !(flags & (FLOWX_FLAG_EXACT | FLOWX_FLAG_REFERENCE_ORDER))) ? 1 : 0;
+    d.x_order = (flags & (FLOWX_FLAG_EXACT | FLOWX_FLAG_REFERENCE_ORDER)) ? 0 : 1;
     if (segs.size() > 1) {
       const int need = (int)segs.size();
       if (need > cseg_count) {
