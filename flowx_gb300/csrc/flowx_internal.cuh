@@ -2,7 +2,8 @@
 //
 // Device-side data layout (HBM):
 //   particle arrays live in *grid order*: slot k holds the particle whose
-//   (cell, id) is the k-th smallest under the last grid build, so the 3x3x3
+//   (cell, id) is the k-th smallest under the last grid build ((cell,
+//   predicted x) in the re-associated arithmetic's fused build), so the 3x3x3
 //   neighbour stencil of any particle is nine contiguous runs of slots (the
 //   three x-adjacent cells of one (y, z) row are adjacent in memory).
 //   ids[k] maps a slot back to the caller's particle id; every upload and

@@ -21,8 +21,9 @@
 // membership equal the reference's; within a cell the reference's bitonic
 // network leaves an arbitrary order, this leaves ascending ids. The fused
 // substep's build in the re-associated arithmetic (x_order) orders each cell
-// by predicted x instead (ties by old slot), so that the slots of a stencil row
-// run in x and the neighbour passes can trim a row to the particle's reach.
+// by predicted x instead (ties by old slot): the slots of a stencil row then run
+// in x, so the walk on coarse cells can trim a row to the particle's reach, and
+// on cells of h a warp's lanes have more alike neighbourhoods.
 #include "pbf_math.cuh"
 
 namespace flowx {

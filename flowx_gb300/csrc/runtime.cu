@@ -368,8 +368,9 @@ int Ctx::upload_segs(const std::vector<SegParams> &s_in, int cells)
 }
 
 // ------------------------------------------------------------ grid build
-// Cell order from the keys and the scan: the counting sort's (cell, id)
-// order, or the reference's own network (FLOWX_FLAG_REFERENCE_ORDER).
+// Cell order from the keys and the scan: the counting sort's (cell, id) or
+// (cell, predicted x) order, or the reference's own network
+// (FLOWX_FLAG_REFERENCE_ORDER).
 void Ctx::issue_cell_order(bool x_order)
 {
   if (flags & FLOWX_FLAG_REFERENCE_ORDER) {
