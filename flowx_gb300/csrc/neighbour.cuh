@@ -163,28 +163,88 @@ struct RowTrim {
   const float4 *__restrict__ row_yz;       // per cell: y, z bounds of its x-row neighbourhood
 };
 
+// Compare-exchange of the descending row-key sort: the larger key first.
+__device__ __forceinline__ void row_key_exchange(uint32_t &a, uint32_t &b)
+{
+  const uint32_t hi = max(a, b);
+  b = min(a, b);
+  a = hi;
+}
+
 // build_row_masks over the slot quads: the same masks, four candidates per
 // three 16-byte loads. A row [ra, rb) is covered by the quads ra/4 .. (rb-1)/4;
 // their accept bits are assembled in order, the ra % 4 bits of slots before
 // ra shifted out and the bits from rb - ra on (slots past the row) cleared.
+//
+// Each lane tests its rows longest first. The masks do not depend on the
+// order rows are tested in (each is stored at its own row), but a warp steps
+// through each row as long as its busiest lane does: with the rows in stencil
+// order the lanes' long rows fall on different steps (lanes in different
+// cells, and particles whose current cell is not the one their slot is in),
+// with them sorted the long rows run together. The rows' quad counts are read
+// first (all eighteen bounds loads issued at once; each row's bounds wait in
+// its mask slot), sorted as keys (count << 4 | row) by a 25-comparator
+// network for nine inputs (each comparator a min and a max; it permutes the
+// keys, so every row is still tested once), and the rows tested in that order.
 template <bool EXACT>
 __device__ __forceinline__ bool build_row_masks_quads(const SegParams &s, const uint32_t *__restrict__ off,
                                                       const SlotQuad *__restrict__ quads, float4 p, float lim2,
                                                       int3 base, unsigned long long *mine, int stride)
 {
   const int x0 = max(base.x - 1, 0), x1 = min(base.x + 1, s.nx - 1);
-  const float2 npx = make_float2(-p.x, -p.x), npy = make_float2(-p.y, -p.y), npz = make_float2(-p.z, -p.z);
-#pragma unroll 1
+  uint32_t key[kRows];
+#pragma unroll
   for (int r = 0; r < kRows; ++r) {
     const int z = base.z + (r / 3) - 1;
     const int y = base.y + (r % 3) - 1;
-    unsigned long long mm = 0ull;
+    uint32_t ra = 0u, rb = 0u;
     if (z >= 0 && z < s.nz && y >= 0 && y < s.ny) {
       const int row = s.c_begin + (z * s.ny + y) * s.nx;
-      const uint32_t ra = __ldg(&off[row + x0]);
-      const uint32_t rb = __ldg(&off[row + x1 + 1]);
+      ra = __ldg(&off[row + x0]);
+      rb = __ldg(&off[row + x1 + 1]);
+      if (rb - ra > 64u) return false;
+    }
+    const uint32_t nq = rb != ra ? ((rb + 3u) >> 2) - (ra >> 2) : 0u;
+    key[r] = (nq << 4) | (uint32_t)r;
+    mine[r * stride] = ((unsigned long long)rb << 32) | ra;  // the row's bounds until its mask replaces them
+  }
+  row_key_exchange(key[0], key[1]);
+  row_key_exchange(key[3], key[4]);
+  row_key_exchange(key[6], key[7]);
+  row_key_exchange(key[1], key[2]);
+  row_key_exchange(key[4], key[5]);
+  row_key_exchange(key[7], key[8]);
+  row_key_exchange(key[0], key[1]);
+  row_key_exchange(key[3], key[4]);
+  row_key_exchange(key[6], key[7]);
+  row_key_exchange(key[0], key[3]);
+  row_key_exchange(key[3], key[6]);
+  row_key_exchange(key[0], key[3]);
+  row_key_exchange(key[1], key[4]);
+  row_key_exchange(key[4], key[7]);
+  row_key_exchange(key[1], key[4]);
+  row_key_exchange(key[2], key[5]);
+  row_key_exchange(key[5], key[8]);
+  row_key_exchange(key[2], key[5]);
+  row_key_exchange(key[1], key[3]);
+  row_key_exchange(key[5], key[7]);
+  row_key_exchange(key[2], key[6]);
+  row_key_exchange(key[4], key[6]);
+  row_key_exchange(key[2], key[4]);
+  row_key_exchange(key[2], key[3]);
+  row_key_exchange(key[5], key[6]);
+  unsigned long long order = 0ull;  // the rows, longest first, four bits each
+#pragma unroll
+  for (int j = 0; j < kRows; ++j) order |= (unsigned long long)(key[j] & 15u) << (4 * j);
+  const float2 npx = make_float2(-p.x, -p.x), npy = make_float2(-p.y, -p.y), npz = make_float2(-p.z, -p.z);
+#pragma unroll 1
+  for (int j = 0; j < kRows; ++j, order >>= 4) {
+    const int r = (int)(order & 15ull);
+    const unsigned long long bounds = mine[r * stride];
+    const uint32_t ra = (uint32_t)bounds, rb = (uint32_t)(bounds >> 32);
+    unsigned long long mm = 0ull;
+    {
       const uint32_t len = rb - ra;
-      if (len > 64u) return false;
       if (len != 0u) {
         const uint32_t lead = ra & 3u;
         const uint32_t g0 = ra >> 2, g1 = (rb + 3u) >> 2;
