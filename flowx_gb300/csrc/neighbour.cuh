@@ -305,6 +305,22 @@ struct MaskRecord {
 };
 
 
+// The first t in [lo, hi) for which pred(t) is false, or hi, for a pred that
+// is true on a prefix of the range and false after it (a binary search).
+template <class P>
+__device__ __forceinline__ uint32_t first_false(uint32_t lo, uint32_t hi, P &&pred)
+{
+#pragma unroll 1
+  while (lo < hi) {
+    const uint32_t mid = lo + ((hi - lo) >> 1);
+    if (pred(mid))
+      lo = mid + 1u;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
 // The walk for cells coarser than the reach (rows of more than 64 slots):
 // each stencil row's run trimmed to the particle's reach, then tested and
 // visited sixteen quads at a time (a 64-bit mask in registers per chunk,
@@ -316,7 +332,8 @@ struct MaskRecord {
 //   sqrt(reach^2 - g^2): the leading quads whose slots all lie left of
 //   p.x - rx (the x-row's running maximum of x at their last slot says so)
 //   and the trailing ones whose slots all lie right of p.x + rx (the running
-//   minimum at their first slot) hold none.
+//   minimum at their first slot) hold none. Both runs are monotone along the
+//   row, so the first quad kept and the last are found by binary search.
 // reach^2 is the test's lim2 widened by 2^-10 and the x window by 2^-20
 // (|p.x| + rx), far above the rounding of the test and of these bounds, so
 // every candidate the test accepts is visited, in the untrimmed walk's order.
@@ -382,10 +399,13 @@ __device__ __forceinline__ void for_each_within_trimmed(const SegParams &s, cons
     const float rx = sqrtf(rx2);
     const float tol = (fabsf(p.x) + rx) * 0x1p-20f;
     const float xlo = p.x - rx - tol, xhi = p.x + rx + tol;
-#pragma unroll 1
-    while (t0 < t1 && 4u * t0 + 3u < rb && __ldg(&trim.quad_bounds[t0].x) < xlo) ++t0;
-#pragma unroll 1
-    while (t1 > t0 && 4u * (t1 - 1u) >= ra && __ldg(&trim.quad_bounds[t1 - 1u].y) > xhi) --t1;
+    // leading quads whose last slot is in the row and whose running maximum
+    // is left of the window; trailing quads whose first slot is in the row
+    // and whose running minimum is right of it (both runs monotone in t)
+    t0 = first_false(t0, min(t1, rb >> 2), [&](uint32_t t) { return __ldg(&trim.quad_bounds[t].x) < xlo; });
+    const uint32_t lo_t = max(t0, (ra + 3u) >> 2);
+    if (lo_t < t1)
+      t1 = first_false(lo_t, t1, [&](uint32_t t) { return !(__ldg(&trim.quad_bounds[t].y) > xhi); });
 #pragma unroll 1
     for (uint32_t c0 = t0; c0 < t1; c0 += 16u) {
       const uint32_t c1 = min(c0 + 16u, t1), nq = c1 - c0;
