@@ -171,6 +171,36 @@ __device__ __forceinline__ void row_key_exchange(uint32_t &a, uint32_t &b)
   a = hi;
 }
 
+// The nine row keys sorted in descending order by a 25-comparator network.
+__device__ __forceinline__ void sort_row_keys(uint32_t (&key)[kRows])
+{
+  row_key_exchange(key[0], key[1]);
+  row_key_exchange(key[3], key[4]);
+  row_key_exchange(key[6], key[7]);
+  row_key_exchange(key[1], key[2]);
+  row_key_exchange(key[4], key[5]);
+  row_key_exchange(key[7], key[8]);
+  row_key_exchange(key[0], key[1]);
+  row_key_exchange(key[3], key[4]);
+  row_key_exchange(key[6], key[7]);
+  row_key_exchange(key[0], key[3]);
+  row_key_exchange(key[3], key[6]);
+  row_key_exchange(key[0], key[3]);
+  row_key_exchange(key[1], key[4]);
+  row_key_exchange(key[4], key[7]);
+  row_key_exchange(key[1], key[4]);
+  row_key_exchange(key[2], key[5]);
+  row_key_exchange(key[5], key[8]);
+  row_key_exchange(key[2], key[5]);
+  row_key_exchange(key[1], key[3]);
+  row_key_exchange(key[5], key[7]);
+  row_key_exchange(key[2], key[6]);
+  row_key_exchange(key[4], key[6]);
+  row_key_exchange(key[2], key[4]);
+  row_key_exchange(key[2], key[3]);
+  row_key_exchange(key[5], key[6]);
+}
+
 // build_row_masks over the slot quads: the same masks, four candidates per
 // three 16-byte loads. A row [ra, rb) is covered by the quads ra/4 .. (rb-1)/4;
 // their accept bits are assembled in order, the ra % 4 bits of slots before
@@ -208,31 +238,7 @@ __device__ __forceinline__ bool build_row_masks_quads(const SegParams &s, const 
     key[r] = (nq << 4) | (uint32_t)r;
     mine[r * stride] = ((unsigned long long)rb << 32) | ra;  // the row's bounds until its mask replaces them
   }
-  row_key_exchange(key[0], key[1]);
-  row_key_exchange(key[3], key[4]);
-  row_key_exchange(key[6], key[7]);
-  row_key_exchange(key[1], key[2]);
-  row_key_exchange(key[4], key[5]);
-  row_key_exchange(key[7], key[8]);
-  row_key_exchange(key[0], key[1]);
-  row_key_exchange(key[3], key[4]);
-  row_key_exchange(key[6], key[7]);
-  row_key_exchange(key[0], key[3]);
-  row_key_exchange(key[3], key[6]);
-  row_key_exchange(key[0], key[3]);
-  row_key_exchange(key[1], key[4]);
-  row_key_exchange(key[4], key[7]);
-  row_key_exchange(key[1], key[4]);
-  row_key_exchange(key[2], key[5]);
-  row_key_exchange(key[5], key[8]);
-  row_key_exchange(key[2], key[5]);
-  row_key_exchange(key[1], key[3]);
-  row_key_exchange(key[5], key[7]);
-  row_key_exchange(key[2], key[6]);
-  row_key_exchange(key[4], key[6]);
-  row_key_exchange(key[2], key[4]);
-  row_key_exchange(key[2], key[3]);
-  row_key_exchange(key[5], key[6]);
+  sort_row_keys(key);
   unsigned long long order = 0ull;  // the rows, longest first, four bits each
 #pragma unroll
   for (int j = 0; j < kRows; ++j) order |= (unsigned long long)(key[j] & 15u) << (4 * j);
@@ -342,26 +348,85 @@ __device__ __forceinline__ uint32_t first_false(uint32_t lo, uint32_t hi, P &&pr
 // x-ordered cells of the re-associated build make the trimmed runs short. A
 // row above the reference's MAX_CELL_SCAN is walked cell by cell with the
 // cap, as for_each_within_rows does.
-//
-// REC: also records the non-empty chunks (mask and first slot) of slot i in
-// rec, so that a later pass over the same positions can replay them.
-// STAGE: the chunks are kept in shared memory (up to kRows, masks in the row
-// mask slots, first slots after them: trimmed_walk_bytes) and visited after
-// all rows, flattened across chunks; a slot with more chunks, or with a row
-// over MAX_CELL_SCAN, is walked again chunk by chunk.
-template <bool EXACT, bool REC = false, bool STAGE = false, class F>
+
+// One stencil row of the trimmed walk: its run [ra, rb) and the quads
+// [t0, t1) that can hold a candidate within reach (t0 == t1: none). False for
+// a row above MAX_CELL_SCAN, which the caller walks cell by cell with the cap.
+struct TrimmedRow {
+  uint32_t ra, rb, t0, t1;
+};
+
+__device__ __forceinline__ bool trim_row(const SegParams &s, const uint32_t *__restrict__ off, RowTrim trim,
+                                         float4 p, float reach2, int3 base, int x0, int x1, int r, TrimmedRow &t)
+{
+  t.ra = t.rb = t.t0 = t.t1 = 0u;
+  const int z = base.z + (r / 3) - 1;
+  const int y = base.y + (r % 3) - 1;
+  if (z < 0 || z >= s.nz || y < 0 || y >= s.ny) return true;
+  const int row = s.c_begin + (z * s.ny + y) * s.nx;
+  const uint32_t ra = __ldg(&off[row + x0]);
+  const uint32_t rb = __ldg(&off[row + x1 + 1]);
+  t.ra = ra;
+  t.rb = rb;
+  if (rb <= ra) return true;
+  if (rb - ra > (uint32_t)kMaxCellScan) return false;
+  const float4 yz = __ldg(&trim.row_yz[row + base.x]);
+  const float gy = fmaxf(fmaxf(yz.x - p.y, p.y - yz.y), 0.0f);
+  const float gz = fmaxf(fmaxf(yz.z - p.z, p.z - yz.w), 0.0f);
+  const float rx2 = reach2 - (gy * gy + gz * gz);
+  if (!(rx2 > 0.0f)) return true;  // the whole row beyond reach
+  uint32_t t0 = ra >> 2, t1 = (rb + 3u) >> 2;
+  const float rx = sqrtf(rx2);
+  const float tol = (fabsf(p.x) + rx) * 0x1p-20f;
+  const float xlo = p.x - rx - tol, xhi = p.x + rx + tol;
+  // leading quads whose last slot is in the row and whose running maximum
+  // is left of the window; trailing quads whose first slot is in the row
+  // and whose running minimum is right of it (both runs monotone in t)
+  t0 = first_false(t0, min(t1, rb >> 2), [&](uint32_t q) { return __ldg(&trim.quad_bounds[q].x) < xlo; });
+  const uint32_t lo_t = max(t0, (ra + 3u) >> 2);
+  if (lo_t < t1)
+    t1 = first_false(lo_t, t1, [&](uint32_t q) { return !(__ldg(&trim.quad_bounds[q].y) > xhi); });
+  t.t0 = t0;
+  t.t1 = t1;
+  return true;
+}
+
+// The accept bits of the quads [c0, c1) (at most 16) of a row [ra, rb): each
+// quad enters a 64-bit window (hi:lo) from the top, so after the last, slot
+// 4 c0 + s sits at bit 64 - 4 (c1 - c0) + s; slots outside the row cleared.
+template <bool EXACT>
+__device__ __forceinline__ unsigned long long chunk_mask(const SlotQuad *__restrict__ quads, float2 npx, float2 npy,
+                                                         float2 npz, float lim2, uint32_t c0, uint32_t c1,
+                                                         uint32_t ra, uint32_t rb)
+{
+  uint32_t lo = 0u, hi = 0u;
+#pragma unroll 1
+  for (uint32_t g = c0; g < c1; ++g) {
+    const float4 X = __ldg(&quads[g].x), Y = __ldg(&quads[g].y), Z = __ldg(&quads[g].z);
+    const float2 a = pair_r2_x2<EXACT>(make_float2(X.x, X.y), make_float2(Y.x, Y.y), make_float2(Z.x, Z.y),
+                                       npx, npy, npz);
+    const float2 b = pair_r2_x2<EXACT>(make_float2(X.z, X.w), make_float2(Y.z, Y.w), make_float2(Z.z, Z.w),
+                                       npx, npy, npz);
+    const uint32_t nib =
+        (a.x < lim2 ? 1u : 0u) | (a.y < lim2 ? 2u : 0u) | (b.x < lim2 ? 4u : 0u) | (b.y < lim2 ? 8u : 0u);
+    lo = __funnelshift_r(lo, hi, 4);
+    hi = (hi >> 4) | (nib << 28);
+  }
+  const uint32_t nq = c1 - c0;
+  unsigned long long m = (((unsigned long long)hi << 32) | lo) >> (64u - 4u * nq);
+  const uint32_t wb = 4u * c0;
+  if (ra > wb) m &= ~((1ull << (ra - wb)) - 1ull);       // slots before the row
+  if (rb - wb < 4u * nq) m &= (1ull << (rb - wb)) - 1ull;  // slots past it
+  return m;
+}
+
+// The trimmed walk visiting as it tests: rows in order, each trimmed row's
+// chunks tested and their set bits visited at once.
+template <bool EXACT, class F>
 __device__ __forceinline__ void for_each_within_trimmed(const SegParams &s, const uint32_t *__restrict__ off,
                                                         const SlotQuad *__restrict__ quads, RowTrim trim, float4 p,
-                                                        float lim2, int3 base, F &&f, MaskRecord rec = {}, int i = 0)
+                                                        float lim2, int3 base, F &&f)
 {
-  uint32_t recorded = 0;
-  bool unrecorded = false;
-  extern __shared__ unsigned long long row_masks[];
-  unsigned long long *sm = row_masks + threadIdx.x;
-  uint32_t *sb = reinterpret_cast<uint32_t *>(row_masks + kRows * blockDim.x) + threadIdx.x;
-  const int stride = blockDim.x;
-  uint32_t staged = 0;
-  bool overflow = false;
   const int x0 = max(base.x - 1, 0), x1 = min(base.x + 1, s.nx - 1);
   const float2 npx = make_float2(-p.x, -p.x), npy = make_float2(-p.y, -p.y), npz = make_float2(-p.z, -p.z);
   const float reach2 = lim2 * (1.0f + 0x1p-10f);
@@ -375,11 +440,6 @@ __device__ __forceinline__ void for_each_within_trimmed(const SegParams &s, cons
     const uint32_t rb = __ldg(&off[row + x1 + 1]);
     if (rb <= ra) continue;
     if (rb - ra > (uint32_t)kMaxCellScan) {
-      unrecorded = true;
-      if (STAGE) {  // visited in order by the second walk
-        overflow = true;
-        continue;
-      }
 #pragma unroll 1
       for (int x = x0; x <= x1; ++x) {
         const uint32_t cs = __ldg(&off[row + x]);
@@ -399,9 +459,6 @@ __device__ __forceinline__ void for_each_within_trimmed(const SegParams &s, cons
     const float rx = sqrtf(rx2);
     const float tol = (fabsf(p.x) + rx) * 0x1p-20f;
     const float xlo = p.x - rx - tol, xhi = p.x + rx + tol;
-    // leading quads whose last slot is in the row and whose running maximum
-    // is left of the window; trailing quads whose first slot is in the row
-    // and whose running minimum is right of it (both runs monotone in t)
     t0 = first_false(t0, min(t1, rb >> 2), [&](uint32_t t) { return __ldg(&trim.quad_bounds[t].x) < xlo; });
     const uint32_t lo_t = max(t0, (ra + 3u) >> 2);
     if (lo_t < t1)
@@ -409,8 +466,6 @@ __device__ __forceinline__ void for_each_within_trimmed(const SegParams &s, cons
 #pragma unroll 1
     for (uint32_t c0 = t0; c0 < t1; c0 += 16u) {
       const uint32_t c1 = min(c0 + 16u, t1), nq = c1 - c0;
-      // each quad enters a 64-bit window (hi:lo) from the top; after the
-      // last, slot 4 c0 + s sits at bit 64 - 4 nq + s
       uint32_t lo = 0u, hi = 0u;
 #pragma unroll 1
       for (uint32_t g = c0; g < c1; ++g) {
@@ -428,27 +483,6 @@ __device__ __forceinline__ void for_each_within_trimmed(const SegParams &s, cons
       const uint32_t wb = 4u * c0;
       if (ra > wb) m &= ~((1ull << (ra - wb)) - 1ull);       // slots before the row
       if (rb - wb < 4u * nq) m &= (1ull << (rb - wb)) - 1ull;  // slots past it
-      if (REC && m != 0ull) {
-        if (recorded < (uint32_t)kMaxChunks) {
-          rec.chunk_masks[(size_t)recorded * rec.n + i] = m;
-          rec.chunk_base[(size_t)recorded * rec.n + i] = wb;
-          ++recorded;
-        } else {
-          unrecorded = true;
-        }
-      }
-      if (STAGE) {
-        if (m != 0ull) {
-          if (staged < (uint32_t)kRows) {
-            sm[staged * stride] = m;
-            sb[staged * stride] = wb;
-            ++staged;
-          } else {
-            overflow = true;
-          }
-        }
-        continue;
-      }
 #pragma unroll 1
       while (m) {
         const int t = __ffsll((long long)m) - 1;
@@ -457,26 +491,122 @@ __device__ __forceinline__ void for_each_within_trimmed(const SegParams &s, cons
       }
     }
   }
-  if (REC) rec.wide[i] = unrecorded ? kChunksNotRecorded : (uint8_t)recorded;
-  if (STAGE) {
-    if (overflow) {
-      for_each_within_trimmed<EXACT>(s, off, quads, trim, p, lim2, base, f);
-      return;
-    }
-    uint32_t j = 0, wb = 0;
-    unsigned long long m = 0ull;
+}
+
+// The trimmed walk of the lambda and XSPH passes: every row trimmed first
+// (row order), then the rows' chunks tested, each lane's rows longest first,
+// into staging slots in shared memory that keep the walk's order (a row's
+// chunks follow those of the rows before it; the masks in the row-mask
+// slots, their first slots after them: trimmed_walk_bytes), then the staged
+// chunks visited in that order, flattened across chunks. A warp steps through
+// each row as long as its busiest lane does, and the trimmed rows a lane can
+// reach differ from lane to lane (about four of the nine on the reference's
+// 2.25 h cells, 16-30 quads each); with them sorted the lanes' long rows run
+// together. A particle with more than kRows chunks, or a row over
+// MAX_CELL_SCAN, is walked again by the in-order walk.
+// REC: the non-empty staged chunks (masks and first slots) are also recorded
+// for slot i, in order, so that a later pass over the same positions can
+// replay them (visit_recorded_chunks).
+// Between the passes each row's entry of the first-slot area holds the row's
+// staging slot (bits 24-31), its quad count (12-23) and its first quad
+// kept, less the row's first quad (0-11): at most 129 quads per row, as a
+// row of more than MAX_CELL_SCAN slots leaves.
+template <bool EXACT, bool REC, class F>
+__device__ __forceinline__ void for_each_within_trimmed_staged(const SegParams &s, const uint32_t *__restrict__ off,
+                                                               const SlotQuad *__restrict__ quads, RowTrim trim,
+                                                               float4 p, float lim2, int3 base, F &&f,
+                                                               MaskRecord rec = {}, int i = 0)
+{
+  extern __shared__ unsigned long long row_masks[];
+  unsigned long long *sm = row_masks + threadIdx.x;
+  uint32_t *sb = reinterpret_cast<uint32_t *>(row_masks + kRows * blockDim.x) + threadIdx.x;
+  const int stride = blockDim.x;
+  const int x0 = max(base.x - 1, 0), x1 = min(base.x + 1, s.nx - 1);
+  const float reach2 = lim2 * (1.0f + 0x1p-10f);
+  uint32_t chunks = 0u;
+  bool overflow = false;
 #pragma unroll 1
-    while (true) {
-      if (m == 0ull) {
-        if (j >= staged) break;
-        m = sm[j * stride];
-        wb = sb[j * stride];
-        ++j;
-      }
-      const int t = __ffsll((long long)m) - 1;
-      m &= m - 1ull;
-      f((int)(wb + (uint32_t)t), true);
+  for (int r = 0; r < kRows; ++r) {
+    TrimmedRow t;
+    uint32_t info = 0u;
+    if (!trim_row(s, off, trim, p, reach2, base, x0, x1, r, t)) {
+      overflow = true;
+    } else if (t.t1 > t.t0) {
+      const uint32_t nq = t.t1 - t.t0;
+      info = (min(chunks, 255u) << 24) | (nq << 12) | (t.t0 - (t.ra >> 2));
+      chunks += (nq + 15u) >> 4;
     }
+    sb[r * stride] = info;
+  }
+  if (overflow || chunks > (uint32_t)kRows) {
+    if (REC) rec.wide[i] = kChunksNotRecorded;
+    for_each_within_trimmed<EXACT>(s, off, quads, trim, p, lim2, base, f);
+    return;
+  }
+  uint32_t key[kRows];  // quad count << 4 | row
+#pragma unroll
+  for (int r = 0; r < kRows; ++r) key[r] = (((sb[r * stride] >> 12) & 0xfffu) << 4) | (uint32_t)r;
+  sort_row_keys(key);
+  unsigned long long order = 0ull;  // the rows, longest first, four bits each
+#pragma unroll
+  for (int j = 0; j < kRows; ++j) order |= (unsigned long long)(key[j] & 15u) << (4 * j);
+  const float2 npx = make_float2(-p.x, -p.x), npy = make_float2(-p.y, -p.y), npz = make_float2(-p.z, -p.z);
+#pragma unroll 1
+  for (int j = 0; j < kRows; ++j, order >>= 4) {
+    const int r = (int)(order & 15ull);
+    const uint32_t info = sb[r * stride];
+    const uint32_t nq = (info >> 12) & 0xfffu;
+    if (nq == 0u) break;  // the rows after it hold nothing either
+    const int row = s.c_begin + ((base.z + (r / 3) - 1) * s.ny + (base.y + (r % 3) - 1)) * s.nx;
+    const uint32_t ra = __ldg(&off[row + x0]), rb = __ldg(&off[row + x1 + 1]);
+    const uint32_t t0 = (ra >> 2) + (info & 0xfffu), t1 = t0 + nq;
+    uint32_t slot = info >> 24;
+#pragma unroll 1
+    for (uint32_t c0 = t0; c0 < t1; c0 += 16u, ++slot) {
+      const unsigned long long m = chunk_mask<EXACT>(quads, npx, npy, npz, lim2, c0, min(c0 + 16u, t1), ra, rb);
+      sm[slot * stride] = m;
+    }
+  }
+  // the staged chunks' first slots (every row's entry read first: a chunk's
+  // staging slot may be a later row's entry)
+  uint32_t info[kRows];
+#pragma unroll
+  for (int r = 0; r < kRows; ++r) info[r] = sb[r * stride];
+#pragma unroll
+  for (int r = 0; r < kRows; ++r) {
+    const uint32_t nq = (info[r] >> 12) & 0xfffu;
+    if (nq == 0u) continue;
+    const int row = s.c_begin + ((base.z + (r / 3) - 1) * s.ny + (base.y + (r % 3) - 1)) * s.nx;
+    uint32_t c0 = (__ldg(&off[row + x0]) >> 2) + (info[r] & 0xfffu);
+    const uint32_t c1 = c0 + nq;
+#pragma unroll 1
+    for (uint32_t slot = info[r] >> 24; c0 < c1; c0 += 16u, ++slot) sb[slot * stride] = 4u * c0;
+  }
+  if (REC) {  // the non-empty chunks, in order
+    uint32_t recorded = 0u;
+#pragma unroll 1
+    for (uint32_t k = 0; k < chunks; ++k) {
+      const unsigned long long m = sm[k * stride];
+      if (m == 0ull) continue;
+      rec.chunk_masks[(size_t)recorded * rec.n + i] = m;
+      rec.chunk_base[(size_t)recorded * rec.n + i] = sb[k * stride];
+      ++recorded;
+    }
+    rec.wide[i] = (uint8_t)recorded;
+  }
+  uint32_t j = 0, wb = 0;
+  unsigned long long m = 0ull;
+#pragma unroll 1
+  while (true) {
+    while (m == 0ull && j < chunks) {
+      m = sm[j * stride];
+      wb = sb[j * stride];
+      ++j;
+    }
+    if (m == 0ull) break;
+    const int b = __ffsll((long long)m) - 1;
+    m &= m - 1ull;
+    f((int)(wb + (uint32_t)b), true);
   }
 }
 
@@ -486,7 +616,7 @@ inline size_t trimmed_walk_bytes(int block)
   return (size_t)block * kRows * (sizeof(unsigned long long) + sizeof(uint32_t));
 }
 
-// Phase 2 from slot i's recorded chunks (for_each_within_trimmed with REC,
+// Phase 2 from slot i's recorded chunks (for_each_within_trimmed_staged with REC,
 // left by the launch just before on the same stream: same positions, grid
 // and reach), flattened across chunks; a slot marked kChunksNotRecorded walks
 // its trimmed rows again.
@@ -504,7 +634,7 @@ __device__ __forceinline__ void visit_recorded_chunks(const SegParams &s, const 
   unsigned long long m = 0ull;
 #pragma unroll 1
   while (true) {
-    if (m == 0ull) {
+    if (m == 0ull) {  // (every recorded chunk holds a candidate)
       if (j >= count) break;
       m = __ldg(&rec.chunk_masks[(size_t)j * rec.n + i]);
       wb = __ldg(&rec.chunk_base[(size_t)j * rec.n + i]);
@@ -569,7 +699,7 @@ __device__ __forceinline__ void for_each_within(const SegParams &s, const uint32
                                                 RowTrim trim, float4 p, float lim2, int3 base, F &&f)
 {
   if (TRIMMED) {
-    for_each_within_trimmed<EXACT, false, true>(s, off, quads, trim, p, lim2, base, f);
+    for_each_within_trimmed_staged<EXACT, false>(s, off, quads, trim, p, lim2, base, f);
     return;
   }
   extern __shared__ unsigned long long row_masks[];
@@ -589,7 +719,7 @@ __device__ __forceinline__ void for_each_within_recording(const SegParams &s, co
                                                           float lim2, int3 base, MaskRecord rec, int i, F &&f)
 {
   if (TRIMMED) {
-    for_each_within_trimmed<EXACT, true, true>(s, off, quads, trim, p, lim2, base, f, rec, i);
+    for_each_within_trimmed_staged<EXACT, true>(s, off, quads, trim, p, lim2, base, f, rec, i);
     return;
   }
   extern __shared__ unsigned long long row_masks[];
