@@ -194,13 +194,28 @@ __global__ void __launch_bounds__(kRowBoundsBlock) k_row_bounds(DeviceState d, c
     float ylo = inf, yhi = -inf, zlo = inf, zhi = -inf;
     if (x >= 0 && x < s.nx) {
       const uint32_t a = __ldg(&off[row + x]), b = __ldg(&off[row + x + 1]);
+      // the cell's particles eight at a time, their loads issued together
+      // (past the cell's end a NaN, which fminf / fmaxf skip)
+      const float nan = __int_as_float(0x7fc00000);
 #pragma unroll 1
-      for (uint32_t k = a; k < b; ++k) {
-        const float4 q = __ldg(&pred[k]);
-        ylo = fminf(ylo, q.y);
-        yhi = fmaxf(yhi, q.y);
-        zlo = fminf(zlo, q.z);
-        zhi = fmaxf(zhi, q.z);
+      for (uint32_t k = a; k < b; k += 8u) {
+        float qy[8], qz[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          qy[u] = qz[u] = nan;
+          if (k + u < b) {
+            const float4 q = __ldg(&pred[k + u]);
+            qy[u] = q.y;
+            qz[u] = q.z;
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          ylo = fminf(ylo, qy[u]);
+          yhi = fmaxf(yhi, qy[u]);
+          zlo = fminf(zlo, qz[u]);
+          zhi = fmaxf(zhi, qz[u]);
+        }
       }
     }
     const float ylo_l = __shfl_up_sync(full, ylo, 1), ylo_r = __shfl_down_sync(full, ylo, 1);
@@ -212,19 +227,19 @@ __global__ void __launch_bounds__(kRowBoundsBlock) k_row_bounds(DeviceState d, c
                                       fminf(zlo, fminf(zlo_l, zlo_r)), fmaxf(zhi, fmaxf(zhi_l, zhi_r)));
   }
   const uint32_t A = __ldg(&off[row]), B = __ldg(&off[row + s.nx]);
-  // running maximum from the first slot, four 32-slot chunks per step (their
+  // running maximum from the first slot, eight 32-slot chunks per step (their
   // loads issued together)
   float carry = -inf;
 #pragma unroll 1
-  for (uint32_t b0 = A; b0 < B; b0 += 128u) {
-    float v[4];
+  for (uint32_t b0 = A; b0 < B; b0 += 256u) {
+    float v[8];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < 8; ++u) {
       const uint32_t k = b0 + 32u * (uint32_t)u + (uint32_t)lane;
       v[u] = k < B ? __ldg(&pred[k]).x : -inf;
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < 8; ++u) {
       const uint32_t k = b0 + 32u * (uint32_t)u + (uint32_t)lane;
       float x = v[u];
 #pragma unroll
@@ -240,15 +255,15 @@ __global__ void __launch_bounds__(kRowBoundsBlock) k_row_bounds(DeviceState d, c
   // running minimum from the last slot
   carry = inf;
 #pragma unroll 1
-  for (uint32_t t0 = 0; t0 < B - A; t0 += 128u) {
-    float v[4];
+  for (uint32_t t0 = 0; t0 < B - A; t0 += 256u) {
+    float v[8];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < 8; ++u) {
       const uint32_t t = t0 + 32u * (uint32_t)u + (uint32_t)lane;  // slots from the x-row's last
       v[u] = t < B - A ? __ldg(&pred[B - 1u - t]).x : inf;
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < 8; ++u) {
       const uint32_t t = t0 + 32u * (uint32_t)u + (uint32_t)lane;
       const uint32_t k = B - 1u - t;
       float x = v[u];
