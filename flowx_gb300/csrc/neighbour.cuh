@@ -647,15 +647,53 @@ __device__ __forceinline__ void visit_recorded_chunks(const SegParams &s, const 
 }
 
 // Phase 2: every set bit of every row, rows in order, slots ascending; each
-// lane moves to its next row when its current mask runs out.
-template <class F>
+// lane moves to its next row when its current mask runs out. WORDS32: the
+// current row's mask is taken as two 32-bit words (bits of slots ra + 0..31,
+// then ra + 32..63), whose first set bit and clear are cheaper than the 64-bit
+// ones; it pays where the body is short (delta_apply: 0.603 -> 0.593 ms on the
+// 4M workload), not in lambda or XSPH (within 0.5%, slower).
+template <bool WORDS32 = false, class F>
 __device__ __forceinline__ void visit_row_masks(const SegParams &s, const uint32_t *__restrict__ off, int3 base,
                                                 const unsigned long long *mine, int stride, F &&f)
 {
   const int x0 = max(base.x - 1, 0);
   int r = -1;
-  unsigned long long m = 0ull;
   uint32_t ra = 0;
+  if (WORDS32) {
+    uint32_t lo = 0u, hi = 0u;
+#pragma unroll 1
+    while (true) {
+      if (lo == 0u) {
+        if (hi != 0u) {
+          lo = hi;
+          hi = 0u;
+          ra += 32u;
+        } else {
+          unsigned long long m = 0ull;
+          do {
+            ++r;
+          } while (r < kRows && (m = mine[r * stride]) == 0ull);
+          if (r >= kRows) break;
+          const int z = base.z + (r / 3) - 1;
+          const int y = base.y + (r % 3) - 1;
+          const int row = s.c_begin + (z * s.ny + y) * s.nx;
+          ra = __ldg(&off[row + x0]);
+          lo = (uint32_t)m;
+          hi = (uint32_t)(m >> 32);
+          if (lo == 0u) {
+            lo = hi;
+            hi = 0u;
+            ra += 32u;
+          }
+        }
+      }
+      const int t = __ffs(lo) - 1;
+      lo &= lo - 1u;
+      f((int)ra + t, true);
+    }
+    return;
+  }
+  unsigned long long m = 0ull;
 #pragma unroll 1
   while (true) {
     if (m == 0ull) {
@@ -758,7 +796,7 @@ __device__ __forceinline__ void for_each_within_recorded(const SegParams &s, con
   }
 #pragma unroll
   for (int r = 0; r < kRows; ++r) mine[r * stride] = __ldg(&rec.masks[(size_t)r * rec.n + i]);
-  visit_row_masks(s, off, base, mine, stride, f);
+  visit_row_masks<true>(s, off, base, mine, stride, f);
 }
 
 // sph_velocity.glsl:20-23 for one slot.
