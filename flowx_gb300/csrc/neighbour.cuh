@@ -509,8 +509,9 @@ __device__ __forceinline__ void for_each_within_trimmed(const SegParams &s, cons
 // replay them (visit_recorded_chunks).
 // Between the passes each row's entry of the first-slot area holds the row's
 // staging slot (bits 24-31), its quad count (12-23) and its first quad
-// kept, less the row's first quad (0-11): at most 129 quads per row, as a
-// row of more than MAX_CELL_SCAN slots leaves.
+// kept, less the row's first quad (0-11): at most 129 quads each, since a
+// row of more than MAX_CELL_SCAN slots sends the particle to the in-order
+// walk.
 template <bool EXACT, bool REC, class F>
 __device__ __forceinline__ void for_each_within_trimmed_staged(const SegParams &s, const uint32_t *__restrict__ off,
                                                                const SlotQuad *__restrict__ quads, RowTrim trim,

@@ -327,7 +327,7 @@ int Ctx::upload_segs(const std::vector<SegParams> &s_in, int cells)
     d.seg0 = segs.empty() ? SegParams{} : segs[0];
     // Cells coarser than the reach (1.5 h or more): the thread-per-particle
     // neighbour passes trim each stencil row to the particle's reach
-    // (for_each_within_trimmed); cells of h keep the untrimmed walk. The
+    // (for_each_within_trimmed_staged); cells of h keep the untrimmed walk. The
     // re-associated arithmetic orders each cell by x, which makes the trimmed
     // runs short and, on cells of h, gives a warp's lanes more alike
     // neighbourhoods (0.6% per frame on the 4M workload); the reference's
