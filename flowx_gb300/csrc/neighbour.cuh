@@ -421,12 +421,17 @@ __device__ __forceinline__ unsigned long long chunk_mask(const SlotQuad *__restr
 }
 
 // The trimmed walk visiting as it tests: rows in order, each trimmed row's
-// chunks tested and their set bits visited at once.
-template <bool EXACT, class F>
+// chunks tested and their set bits visited at once. REC: also records the
+// non-empty chunks (mask and first slot) of slot i, up to kMaxChunks, for a
+// later pass over the same positions (else, or with a row over
+// MAX_CELL_SCAN, the slot is marked kChunksNotRecorded).
+template <bool EXACT, bool REC = false, class F>
 __device__ __forceinline__ void for_each_within_trimmed(const SegParams &s, const uint32_t *__restrict__ off,
                                                         const SlotQuad *__restrict__ quads, RowTrim trim, float4 p,
-                                                        float lim2, int3 base, F &&f)
+                                                        float lim2, int3 base, F &&f, MaskRecord rec = {}, int i = 0)
 {
+  uint32_t recorded = 0u;
+  bool unrecorded = false;
   const int x0 = max(base.x - 1, 0), x1 = min(base.x + 1, s.nx - 1);
   const float2 npx = make_float2(-p.x, -p.x), npy = make_float2(-p.y, -p.y), npz = make_float2(-p.z, -p.z);
   const float reach2 = lim2 * (1.0f + 0x1p-10f);
@@ -440,6 +445,7 @@ __device__ __forceinline__ void for_each_within_trimmed(const SegParams &s, cons
     const uint32_t rb = __ldg(&off[row + x1 + 1]);
     if (rb <= ra) continue;
     if (rb - ra > (uint32_t)kMaxCellScan) {
+      unrecorded = true;
 #pragma unroll 1
       for (int x = x0; x <= x1; ++x) {
         const uint32_t cs = __ldg(&off[row + x]);
@@ -483,6 +489,15 @@ __device__ __forceinline__ void for_each_within_trimmed(const SegParams &s, cons
       const uint32_t wb = 4u * c0;
       if (ra > wb) m &= ~((1ull << (ra - wb)) - 1ull);       // slots before the row
       if (rb - wb < 4u * nq) m &= (1ull << (rb - wb)) - 1ull;  // slots past it
+      if (REC && m != 0ull) {
+        if (recorded < (uint32_t)kMaxChunks) {
+          rec.chunk_masks[(size_t)recorded * rec.n + i] = m;
+          rec.chunk_base[(size_t)recorded * rec.n + i] = wb;
+          ++recorded;
+        } else {
+          unrecorded = true;
+        }
+      }
 #pragma unroll 1
       while (m) {
         const int t = __ffsll((long long)m) - 1;
@@ -491,6 +506,7 @@ __device__ __forceinline__ void for_each_within_trimmed(const SegParams &s, cons
       }
     }
   }
+  if (REC) rec.wide[i] = unrecorded ? kChunksNotRecorded : (uint8_t)recorded;
 }
 
 // The trimmed walk of the lambda and XSPH passes: every row trimmed first
@@ -503,7 +519,8 @@ __device__ __forceinline__ void for_each_within_trimmed(const SegParams &s, cons
 // reach differ from lane to lane (about four of the nine on the reference's
 // 2.25 h cells, 16-30 quads each); with them sorted the lanes' long rows run
 // together. A particle with more than kRows chunks, or a row over
-// MAX_CELL_SCAN, is walked again by the in-order walk.
+// MAX_CELL_SCAN, is walked again by the in-order walk (which records its
+// chunks with REC).
 // REC: the non-empty staged chunks (masks and first slots) are also recorded
 // for slot i, in order, so that a later pass over the same positions can
 // replay them (visit_recorded_chunks).
@@ -540,8 +557,7 @@ __device__ __forceinline__ void for_each_within_trimmed_staged(const SegParams &
     sb[r * stride] = info;
   }
   if (overflow || chunks > (uint32_t)kRows) {
-    if (REC) rec.wide[i] = kChunksNotRecorded;
-    for_each_within_trimmed<EXACT>(s, off, quads, trim, p, lim2, base, f);
+    for_each_within_trimmed<EXACT, REC>(s, off, quads, trim, p, lim2, base, f, rec, i);
     return;
   }
   uint32_t key[kRows];  // quad count << 4 | row
